@@ -1,0 +1,371 @@
+"""Throughput of the scattering hot path on GB300 (one JSON line on rank 0).
+
+Workload: Scattering2D J=3, L=8, max_order=2 on 256x256 float32 Gaussian
+random fields (white N(0,1) smoothed by an isotropic Gaussian of sigma
+U[1,4] px, rescaled to [0,1]; seed 2), batch 64 per GPU.  One step = one
+forward over the batch.  Inputs are generated synthetically (no dataset).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the
+numpy oracle port of kymatio's numpy backend, float32 arithmetic like the
+reference's fp32 path) on the host cores, on a bounded sample per step.
+Under torchrun each rank is an independent replica (images shard with no
+exchange step): value = images over all ranks / max time over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+J, L, SIDE, BATCH = 3, 8, 256, 64
+METRIC = 'Scattering2D 256^2 J=3 L=8 img/s'
+
+
+def grf_batch(n, seed=2, side=SIDE):
+    """Gaussian random fields rescaled to [0,1] (float32)."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, side, side), np.float32)
+    for i in range(n):
+        w = rng.standard_normal((side, side))
+        s = rng.uniform(1.0, 4.0)
+        g = gaussian_filter(w, s, mode='wrap')
+        g = (g - g.min()) / (g.max() - g.min())
+        out[i] = g.astype(np.float32)
+    return out
+
+
+def algorithmic_bytes_per_image(J=J, L=L, side=SIDE):
+    """Compulsory HBM bytes of the plain path per image: input, output and one
+    write + one read of every order-1 parent spectrum (fp32 complex)."""
+    Mp = ((side + 2 ** J) // 2 ** J + 1) * 2 ** J
+    C = 1 + J * L + L * L * J * (J - 1) // 2
+    out = 4 * C * (side // 2 ** J) ** 2
+    spill = 2 * 8 * L * sum((Mp // 2 ** j1) ** 2 for j1 in range(J - 1))
+    return 4 * side * side + out + spill
+
+
+def fft_flops_per_image(J=J, L=L, side=SIDE):
+    """5 n log2 n convention over every 2-D FFT of the cascade."""
+    Mp = ((side + 2 ** J) // 2 ** J + 1) * 2 ** J
+    f = lambda m: 5.0 * m * m * math.log2(m * m)
+    s = Mp // 2 ** J
+    tot = f(Mp) + f(s)
+    for j1 in range(J):
+        m1 = Mp >> j1
+        tot += L * (2 * f(m1) + f(s))
+        for j2 in range(j1 + 1, J):
+            m2 = Mp >> j2
+            tot += L * L * (2 * f(m2) + f(s))
+    return tot
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index, self.proc, self.path = index, None, None
+
+    def start(self):
+        try:
+            os.makedirs(os.path.join(ROOT, 'gpurun_out'), exist_ok=True)
+            self.path = os.path.join(ROOT, 'gpurun_out', 'bench_clocks_%d.csv' % os.getpid())
+            self.f = open(self.path, 'w')
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            p = [t.strip() for t in line.split(',')]
+            if len(p) >= 9:
+                rows.append(p)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith('active')})
+        load = [v for v in sm if mx and v > 0.5 * max(mx)] or sm
+        return {'sm_mhz': statistics.median(load) if load else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def cpu_reference_rate(n_img, threads, repeats=1):
+    """Time the reference algorithm (oracle port, float32 like the reference's
+    fp32 numpy path) on n_img images; returns (img/s, seconds)."""
+    import scipy.fft
+    from oracle.scattering2d import Scattering2D as Oracle
+    S = Oracle(J, (SIDE, SIDE), L=L)
+    x = grf_batch(n_img, seed=2)
+    with scipy.fft.set_workers(threads):
+        S(x[:1])
+        best = float('inf')
+        for _ in range(repeats):
+            t = time.perf_counter()
+            S(x)
+            best = min(best, time.perf_counter() - t)
+    return n_img / best, best
+
+
+def dist_init():
+    import torch
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        import torch.distributed as dist
+        backend = 'nccl' if torch.cuda.is_available() else 'gloo'
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device='cuda' if torch.cuda.is_available() else 'cpu')
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = 4
+    # warm-up steps then timed steps, each a bounded sample of the workload
+    for _ in range(args.warmup):
+        cpu_reference_rate(1, threads)
+    times = []
+    for _ in range(args.steps):
+        rate, sec = cpu_reference_rate(n, threads)
+        times.append(sec)
+    value = n * len(times) / sum(times)
+    line = {'metric': METRIC, 'value': value, 'unit': 'img/s', 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1e3 * sum(times) / len(times), 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'impl': 'reference',
+            'config': {'workload': 'Scattering2D J=3 L=8 max_order=2 256x256 GRF, %d-image sample per step' % n,
+                       'global_batch': BATCH, 'parallelism': 'host cores'},
+            'cpu_baseline': {'value': value, 'unit': 'img/s', 'cores': threads, 'kind': 'port',
+                             'sample': '%d images per step, oracle port of the reference numpy backend, '
+                                       'fp32, scipy.fft workers=%d' % (n, threads)},
+            'e2e': {'value': value, 'unit': 'img/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import ctypes
+    import torch
+    from kymatio_gb300 import Scattering2D, _lib
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    lib = _lib.load()
+    x_host = torch.from_numpy(grf_batch(BATCH, seed=2 + rank)).pin_memory()
+    x = x_host.to(dev)
+    S = Scattering2D(J, (SIDE, SIDE), L=L).to(dev)
+    if args.chunk:
+        S.set_chunk(args.chunk)
+    plan = S._get_plan()
+    ngroups = lib.kym_s2d_group_count(plan.h)
+    ginfo = []
+    for g in range(ngroups):
+        v = [ctypes.c_int() for _ in range(6)]
+        lib.kym_s2d_group_info(plan.h, g, *[ctypes.byref(i) for i in v])
+        ginfo.append([i.value for i in v])
+    chunk = lib.kym_s2d_get_chunk(plan.h)
+    n_chunks = -(-BATCH // min(chunk, BATCH))
+    launches_per_step = sum(1 if gi[0] == 0 else n_chunks for gi in ginfo)
+    out = torch.empty((BATCH, S._channels) + S._out_hw, device=dev)
+    ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, BATCH)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    ptrs = S._filter_ptrs()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
+    stream = torch.cuda.current_stream(dev)
+    gms = (ctypes.c_float * ngroups)()
+
+    def step(timed_groups):
+        if timed_groups:
+            _lib.check(lib.kym_s2d_forward_timed(plan.h, x.data_ptr(), out.data_ptr(), BATCH, ptrs, S._n_filters,
+                                                 ws.data_ptr(), ws_bytes, stream.cuda_stream, gms, ngroups),
+                       'forward_timed')
+        else:
+            _lib.check(lib.kym_s2d_forward(plan.h, x.data_ptr(), out.data_ptr(), BATCH, ptrs, S._n_filters,
+                                           ws.data_ptr(), ws_bytes, stream.cuda_stream), 'forward')
+
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize()
+    # ---- device-timed region: per-step events, L2 flushed between steps ----
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    step_ms = []
+    group_tot = np.zeros(ngroups)
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(False)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    # per-launch kernel durations of every group (same stream, same workload)
+    for _ in range(args.steps):
+        flush.zero_()
+        step(True)
+        group_tot += np.array([gms[i] for i in range(ngroups)])
+    clocks = sampler.stop()
+    t_step = max_over_ranks(sum(step_ms) / len(step_ms), world)
+    value = BATCH * world / (t_step / 1e3)
+    # ---- end to end through the public API: pinned host in, host out -------
+    out_host = torch.empty((BATCH, S._channels) + S._out_hw, dtype=torch.float32).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        out_host.copy_(S(x_host.to(dev, non_blocking=True)), non_blocking=True)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        flush.zero_()
+        out_host.copy_(S(x_host.to(dev, non_blocking=True)), non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    flush_ms = 0.0
+    fe0, fe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fe0.record(stream)
+    for _ in range(args.steps):
+        flush.zero_()
+    fe1.record(stream)
+    torch.cuda.synchronize()
+    flush_ms = fe0.elapsed_time(fe1)
+    e2e_ms = max_over_ranks((e0.elapsed_time(e1) - flush_ms) / args.steps, world)
+    e2e = BATCH * world / (e2e_ms / 1e3)
+    # ---- roofline of the dominant group -------------------------------------
+    per_launch = []
+    for g, gi in enumerate(ginfo):
+        nl = 1 if gi[0] == 0 else n_chunks
+        per_launch.append(group_tot[g] / args.steps / nl)
+    dom = int(np.argmax(group_tot))
+    lvl, ntasks, rows, cols, fold, cl = ginfo[dom]
+    imgs_per_launch = BATCH if lvl == 0 else min(chunk, BATCH)
+    # algorithmic bytes of one launch of that group: per task and image it
+    # reads the parent spectrum and the wavelet (fold^2 * rows*cols complex +
+    # real), the low-pass filter (rows*cols real) and writes its output channel
+    side_out = SIDE // 2 ** J
+    if lvl == 0:
+        bytes_launch = imgs_per_launch * (4 * SIDE * SIDE + 8 * rows * cols + 4 * side_out ** 2)
+    else:
+        src = fold * fold * rows * cols
+        spill_w = 8 * rows * cols if (lvl == 1 and rows > (272 >> (J - 1))) else 0
+        bytes_launch = imgs_per_launch * ntasks * (8 * src + 4 * side_out ** 2 + spill_w) + \
+            ntasks * (4 * src + 4 * rows * cols)
+    dur_s = per_launch[dom] / 1e3
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except Exception:
+        pass
+    hbm_peak = peaks.get('hbm_gbs', 6800.0)
+    achieved = bytes_launch / dur_s / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, 'profiles', 'dominant_traffic.json')
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get('bytes_per_launch')
+        except Exception:
+            traffic = None
+    flops_img = fft_flops_per_image()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, sec = cpu_reference_rate(8, threads)
+        cpu = {'value': rate, 'unit': 'img/s', 'cores': threads, 'kind': 'port',
+               'sample': '8 GRF images (%.1f s), oracle port of the reference numpy backend in fp32, '
+                         'scipy.fft workers=%d' % (sec, threads)}
+    if rank == 0:
+        line = {
+            'metric': METRIC, 'value': value, 'unit': 'img/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': t_step, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': 'Scattering2D J=3 L=8 max_order=2, 256x256 GRF float32, plain FP32 fused path',
+                       'global_batch': BATCH * world, 'per_gpu_batch': BATCH, 'chunk': chunk,
+                       'l2': 'flushed (256 MB write) between timed steps', 'parallelism': 'replicas x%d' % world},
+            'e2e': {'value': e2e, 'unit': 'img/s', 'h2d_bytes_per_step': int(x_host.numel() * 4),
+                    'd2h_bytes_per_step': int(out_host.numel() * 4)},
+            'gpu_launches': launches_per_step * args.steps,
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s',
+                         'frac': achieved / hbm_peak, 'traffic': traffic,
+                         'kernel': 'cascade group %d (level %d, %dx%d, fold %d, cluster %d, %d tasks)'
+                                   % (dom, lvl, rows, cols, fold, cl, ntasks),
+                         'kernel_ms_per_launch': per_launch[dom],
+                         'peak_source': 'measured' if 'hbm_gbs' in peaks else 'fallback'},
+            'fp32_fft': {'gflop_per_img_5nlogn': flops_img / 1e9,
+                         'achieved_tflops': flops_img * value / world / 1e12},
+            'group_ms_per_step': [round(v / args.steps, 4) for v in group_tot],
+            'clocks': clocks,
+            'cpu_baseline': cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--chunk', type=int, default=0)
+    ap.add_argument('--no-cpu', action='store_true')
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == 'reference':
+        world, rank = int(os.environ.get('WORLD_SIZE', '1')), int(os.environ.get('RANK', '0'))
+        run_reference(args, world, rank)
+        return
+    world, rank, local = dist_init()
+    run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,109 @@
+/*
+ * kymatio_gb300 -- C ABI of the GB300 scattering engine (sm_103a).
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*, a cudaStream_t; NULL is the legacy default stream), is
+ * enqueued asynchronously on that stream, and returns an int status
+ * (KYM_OK = 0).  No exception crosses this boundary.  The caller owns every
+ * buffer: inputs, outputs, filters and workspaces are allocated by the caller
+ * (the Python frontend allocates them with torch on the current device).
+ * Tensors are contiguous, C order, float32; complex data is interleaved
+ * (re, im) pairs, i.e. the reference's trailing dimension of 2.
+ *
+ * Plans are host objects holding the transform geometry; they upload small
+ * task/twiddle tables to each device on first use and are safe to share
+ * between threads and streams.
+ */
+#ifndef KYMATIO_GB300_H
+#define KYMATIO_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KYM_OK 0
+#define KYM_ERR_INVALID 1     /* bad argument, shape or pointer */
+#define KYM_ERR_UNSUPPORTED 2 /* geometry the kernels cannot run (e.g. too large for shared memory) */
+#define KYM_ERR_CUDA 3        /* a CUDA call failed (launch, copy, allocation of plan tables) */
+#define KYM_ERR_WORKSPACE 4   /* workspace missing or smaller than required */
+
+/* Library version, "major.minor.patch". */
+const char* kym_version(void);
+/* Message for the last CUDA error this thread saw inside the library. */
+const char* kym_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * 2-D scattering (replaces the forward of ScatteringTorch2D,
+ * kymatio/scattering2d/frontend/torch_frontend.py:72-111, driving
+ * kymatio/scattering2d/core/scattering2d.py:1-88 over the op surface of
+ * kymatio/scattering2d/backend/torch_backend.py:89-180).
+ * ---------------------------------------------------------------------- */
+typedef struct kym_s2d_plan kym_s2d_plan;
+
+/* Geometry of ScatteringBase2D.build (kymatio/scattering2d/frontend/
+ * base_frontend.py:19-32): padding to ((M+2^J)//2^J+1)*2^J.  Returns
+ * KYM_ERR_INVALID when 2^J exceeds M or N (the reference raises
+ * 'The smallest dimension should be larger than 2^J.'). */
+int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, int pre_pad, kym_s2d_plan** plan);
+int kym_s2d_plan_destroy(kym_s2d_plan* plan);
+/* Padded size, output channel count C = 1 + JL + L^2 J(J-1)/2 (max_order 2),
+ * output spatial size and the number of filters the forward expects. */
+int kym_s2d_plan_info(const kym_s2d_plan* plan, int* M_padded, int* N_padded, int* channels, int* out_rows,
+                      int* out_cols, int* n_filters);
+/* Shape of filter `index` in the order of the reference's registered buffers
+ * tensor0..tensorK (kymatio/scattering2d/frontend/torch_frontend.py:28-43):
+ * phi levels 0..J-1, then every psi's levels. */
+int kym_s2d_filter_shape(const kym_s2d_plan* plan, int index, int* rows, int* cols);
+/* Images per pass over the order-2 cascade (sizes the parent-spectrum workspace). */
+int kym_s2d_set_chunk(kym_s2d_plan* plan, int chunk);
+int kym_s2d_get_chunk(const kym_s2d_plan* plan);
+size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch);
+/* The forward runs as launch groups (input stage, one per order-1 scale, one
+ * per order-2 scale pair); these describe them: level 0/1/2, tasks per
+ * image, work size, fold factor from the parent spectrum, CTAs per task. */
+int kym_s2d_group_count(const kym_s2d_plan* plan);
+int kym_s2d_group_info(const kym_s2d_plan* plan, int group, int* level, int* ntasks, int* rows, int* cols, int* fold,
+                       int* cluster);
+/* kym_s2d_forward with CUDA events around every launch; group_ms[g] receives
+ * the summed device time of group g (synchronises the stream). */
+int kym_s2d_forward_timed(const kym_s2d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
+                          int n_filters, void* workspace, size_t workspace_bytes, void* stream, float* group_ms,
+                          int max_groups);
+/* x: (batch, M, N) (or the padded size when pre_pad); out: (batch, C, out_rows,
+ * out_cols); filters: host array of n_filters device pointers (real Fourier
+ * filters, the reference's tensor{n} buffers without their trailing dim). */
+int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
+                    int n_filters, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * 1-D scattering, local averaging (replaces ScatteringBase1D.scattering with
+ * average='local', kymatio/scattering1d/frontend/base_frontend.py:106-155,
+ * and kymatio/scattering1d/core/scattering1d.py:2-107 over
+ * kymatio/scattering1d/backend/torch_backend.py:18-141).  The geometry comes
+ * from the frontend's build(): padded length (a power of two), reflect pad,
+ * log2 of the stride, the j of every first/second-order wavelet and its
+ * number of levels, and the unpad window at the output resolution.
+ * ---------------------------------------------------------------------- */
+typedef struct kym_s1d_plan kym_s1d_plan;
+
+int kym_s1d_plan_create(int N_padded, int N_input, int pad_left, int log2_stride, int max_order, int n_psi1,
+                        const int* psi1_j, const int* psi1_nlevels, int n_psi2, const int* psi2_j,
+                        const int* psi2_nlevels, int n_phi_levels, int out_start, int out_end,
+                        kym_s1d_plan** plan);
+int kym_s1d_plan_destroy(kym_s1d_plan* plan);
+int kym_s1d_plan_info(const kym_s1d_plan* plan, int* channels, int* out_len, int* n_filters);
+int kym_s1d_set_chunk(kym_s1d_plan* plan, int chunk);
+size_t kym_s1d_workspace_bytes(const kym_s1d_plan* plan, int batch);
+/* x: (batch, N_input); out: (batch, channels, out_len); filters ordered as
+ * the reference's tensor{n} buffers (phi levels, psi1 levels, psi2 levels,
+ * kymatio/scattering1d/frontend/torch_frontend.py:30-56). */
+int kym_s1d_forward(const kym_s1d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
+                    int n_filters, void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KYMATIO_GB300_H */

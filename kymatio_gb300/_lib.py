@@ -1,0 +1,98 @@
+"""ctypes binding of the C ABI in ``include/kymatio_gb300.h``.
+
+The shared library is built in-tree (``kymatio_gb300/_lib``) by
+``kymatio_gb300.build``.  There is no fallback: every transform in this
+package runs through these entry points, and a missing library raises.
+"""
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+KYM_OK = 0
+KYM_ERR_INVALID = 1
+KYM_ERR_UNSUPPORTED = 2
+KYM_ERR_CUDA = 3
+KYM_ERR_WORKSPACE = 4
+
+_ERRNAMES = {KYM_ERR_INVALID: 'invalid argument', KYM_ERR_UNSUPPORTED: 'unsupported geometry',
+             KYM_ERR_CUDA: 'CUDA error', KYM_ERR_WORKSPACE: 'workspace too small'}
+
+_c_int, _c_size, _vp = ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p
+_ip = ctypes.POINTER(ctypes.c_int)
+
+# name -> (restype, argtypes); the full list of exported entry points
+SIGNATURES = {
+    'kym_version': (ctypes.c_char_p, []),
+    'kym_last_error': (ctypes.c_char_p, []),
+    'kym_s2d_plan_create': (_c_int, [_c_int] * 6 + [ctypes.POINTER(_vp)]),
+    'kym_s2d_plan_destroy': (_c_int, [_vp]),
+    'kym_s2d_plan_info': (_c_int, [_vp] + [_ip] * 6),
+    'kym_s2d_filter_shape': (_c_int, [_vp, _c_int, _ip, _ip]),
+    'kym_s2d_set_chunk': (_c_int, [_vp, _c_int]),
+    'kym_s2d_get_chunk': (_c_int, [_vp]),
+    'kym_s2d_workspace_bytes': (_c_size, [_vp, _c_int]),
+    'kym_s2d_forward': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
+    'kym_s2d_group_count': (_c_int, [_vp]),
+    'kym_s2d_group_info': (_c_int, [_vp, _c_int] + [_ip] * 6),
+    'kym_s2d_forward_timed': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp,
+                                       ctypes.POINTER(ctypes.c_float), _c_int]),
+    'kym_s1d_plan_create': (_c_int, [_c_int] * 6 + [_ip, _ip, _c_int, _ip, _ip, _c_int, _c_int, _c_int,
+                                                   ctypes.POINTER(_vp)]),
+    'kym_s1d_plan_destroy': (_c_int, [_vp]),
+    'kym_s1d_plan_info': (_c_int, [_vp, _ip, _ip, _ip]),
+    'kym_s1d_set_chunk': (_c_int, [_vp, _c_int]),
+    'kym_s1d_workspace_bytes': (_c_size, [_vp, _c_int]),
+    'kym_s1d_forward': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=False):
+    """Load (once) and return the ctypes handle of the library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = lib_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise RuntimeError(
+                    'kymatio_gb300 CUDA library not built (%s missing); run '
+                    '`python -m kymatio_gb300.build`' % path)
+            _build.build()
+        h = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+        return h
+
+
+class KymError(RuntimeError):
+    pass
+
+
+def check(status, what):
+    if status != KYM_OK:
+        msg = _ERRNAMES.get(status, 'status %d' % status)
+        if status == KYM_ERR_CUDA:
+            msg += ': ' + load().kym_last_error().decode()
+        raise KymError('%s failed: %s' % (what, msg))
+
+
+def int_array(values):
+    arr = (ctypes.c_int * max(1, len(values)))(*values)
+    return arr
+
+
+def ptr_array(ptrs):
+    return (_vp * max(1, len(ptrs)))(*ptrs)

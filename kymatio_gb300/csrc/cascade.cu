@@ -1,0 +1,880 @@
+// Fused scattering cascade kernels, their host-side plans and the C ABI of
+// the forward transforms (include/kymatio_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <tuple>
+#include <vector>
+
+#include "../../include/kymatio_gb300.h"
+#include "cascade.cuh"
+#include "plan_util.h"
+
+namespace kym {
+
+__device__ __forceinline__ int reflect_idx(int i, int n) {
+  if (n == 1) return 0;
+  const int period = 2 * (n - 1);
+  i %= period;
+  if (i < 0) i += period;
+  return i < n ? i : period - i;
+}
+
+// ---------------------------------------------------------------------------
+// The fused task kernel.  grid = (ntasks * cluster, images), cluster = (C,1,1)
+// CL: the work array is split over a cluster.  ONED: a single row (1-D).
+// ---------------------------------------------------------------------------
+template <bool CL, bool ONED>
+__global__ void __launch_bounds__(kThreads, 1)
+    cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* A = reinterpret_cast<float2*>(smem_raw);
+  const int C = CL ? L.cluster : 1;
+  int rank = 0;
+  if constexpr (CL) rank = static_cast<int>(cg::this_cluster().block_rank());
+  const int task_id = blockIdx.x / C;
+  const int img = blockIdx.y;
+  const Task t = L.tasks[task_id];
+  const int rl = L.rows_local;
+  const int row0 = rank * rl;
+  const int mc = L.mc;
+  float2* B = A + (size_t)rl * L.ld;
+  float2** rowp = reinterpret_cast<float2**>(B + (size_t)L.sr * L.ldb);
+
+  Slab w;
+  w.local = A;
+  w.rowp = rowp;
+  w.rows = L.mr;
+  w.cols = mc;
+  w.ld = L.ld;
+  w.rows_local = rl;
+  w.row0 = row0;
+  w.nct = C;
+  w.rank = rank;
+  const Barrier local_bar{false};
+  const Barrier wide_bar{CL};
+
+  if constexpr (CL) {
+    cg::cluster_group cl = cg::this_cluster();
+    for (int g = threadIdx.x; g < L.mr; g += blockDim.x) {
+      const int owner = g / rl;
+      float2* base = cl.map_shared_rank(A, owner);
+      rowp[g] = base + (size_t)(g - owner * rl) * L.ld;
+    }
+  }
+
+  auto elem = [&](int u, int v) -> float2* {
+    if constexpr (ONED) return A + (v + (v >> 4));
+    else return A + (size_t)u * L.ld + v;
+  };
+
+  // ---- load: reflect-padded image, or fold(src * psi) -----------------------
+  const int nloc = rl * mc;
+  if (L.src_image) {
+    const float* x = L.x + (size_t)(L.img0 + img) * L.x_stride;
+    for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
+      const int u = e / mc, v = e - (e / mc) * mc;
+      const int iy = ONED ? 0 : reflect_idx(row0 + u - L.pad_t, L.img_M);
+      const int ix = reflect_idx(v - L.pad_l, L.img_N);
+      *elem(u, v) = make_float2(__ldg(x + (size_t)iy * L.img_N + ix) * L.load_scale, 0.f);
+    }
+  } else {
+    const float2* src = L.src + (size_t)img * L.src_stride + t.src_off;
+    const float* psi = t.psi >= 0 ? F.f[t.psi] : nullptr;
+    const int scols = L.kc * mc;
+    for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
+      const int u = e / mc, v = e - (e / mc) * mc;
+      const int gu = row0 + u;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int a = 0; a < L.kr; ++a) {
+        const size_t rbase = (size_t)(gu + a * L.mr) * scols + v;
+        for (int b = 0; b < L.kc; ++b) {
+          const size_t idx = rbase + (size_t)b * mc;
+          const float2 s = __ldg(src + idx);
+          const float f = psi ? __ldg(psi + idx) : 1.f;
+          acc.x = fmaf(s.x, f, acc.x);
+          acc.y = fmaf(s.y, f, acc.y);
+        }
+      }
+      *elem(u, v) = cscale(acc, L.load_scale);
+    }
+  }
+  __syncthreads();
+
+  const int cpc = mc / C;  // columns handled by this CTA in column passes
+  if (L.modulus) {
+    // U = |IFFT2(A)| ; A = FFT2(U)
+    fft_pass<true, ONED, false>(w, rl, 0, L.prow, true, local_bar);
+    if constexpr (!ONED) {
+      if constexpr (CL) cg::this_cluster().sync();
+      fft_pass<false, false, CL>(w, cpc, rank * cpc, L.pcol, true, wide_bar);
+    }
+    for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
+      const int u = e / mc, v = e - (e / mc) * mc;
+      float2* p = elem(u, v);
+      const float2 z = *p;
+      *p = make_float2(sqrtf(z.x * z.x + z.y * z.y), 0.f);
+    }
+    if constexpr (!ONED) {
+      wide_bar.sync();
+      fft_pass<false, false, CL>(w, cpc, rank * cpc, L.pcol, false, wide_bar);
+    } else {
+      __syncthreads();
+    }
+    fft_pass<true, ONED, false>(w, rl, 0, L.prow, false, local_bar);
+  } else {
+    fft_pass<true, ONED, false>(w, rl, 0, L.prow, false, local_bar);
+    if constexpr (!ONED) {
+      if constexpr (CL) cg::this_cluster().sync();
+      fft_pass<false, false, CL>(w, cpc, rank * cpc, L.pcol, false, wide_bar);
+    }
+  }
+
+  // ---- store the spectrum for the next order --------------------------------
+  if (t.dst_off >= 0) {
+    float2* dst = L.dst + (size_t)img * L.dst_stride + t.dst_off + (size_t)row0 * mc;
+    for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
+      const int u = e / mc, v = e - (e / mc) * mc;
+      dst[e] = *elem(u, v);
+    }
+  }
+
+  // ---- low-pass branch: B = fold(A * phi) (partial over local rows) --------
+  const float* phi = F.f[t.phi];
+  const int sr = L.sr, sc = L.sc;
+  const int ksr = L.mr / sr, ksc = mc / sc;
+  for (int e = threadIdx.x; e < sr * sc; e += blockDim.x) {
+    const int p = e / sc, q = e - (e / sc) * sc;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int a = 0; a < ksr; ++a) {
+      const int g = p + a * sr;
+      if (g < row0 || g >= row0 + rl) continue;
+      for (int b = 0; b < ksc; ++b) {
+        const int col = q + b * sc;
+        const float2 z = *elem(g - row0, col);
+        const float f = __ldg(phi + (size_t)g * mc + col);
+        acc.x = fmaf(z.x, f, acc.x);
+        acc.y = fmaf(z.y, f, acc.y);
+      }
+    }
+    float2* bp = ONED ? B + (q + (q >> 4)) : B + (size_t)p * L.ldb + q;
+    *bp = cscale(acc, L.s_scale);
+  }
+  if constexpr (CL) {
+    cg::cluster_group cl = cg::this_cluster();
+    cl.sync();
+    if (rank == 0) {
+      for (int e = threadIdx.x; e < sr * sc; e += blockDim.x) {
+        const int p = e / sc, q = e - (e / sc) * sc;
+        float2* bp = B + (size_t)p * L.ldb + q;
+        float2 acc = *bp;
+        for (int r = 1; r < C; ++r) acc = cadd(acc, *cl.map_shared_rank(bp, r));
+        *bp = acc;
+      }
+    }
+    cl.sync();
+    if (rank != 0) return;
+  }
+  __syncthreads();
+
+  // ---- small inverse transform and unpadded real output ---------------------
+  Slab wb;
+  wb.local = B;
+  wb.rowp = nullptr;
+  wb.rows = sr;
+  wb.cols = sc;
+  wb.ld = L.ldb;
+  wb.rows_local = sr;
+  wb.row0 = 0;
+  wb.nct = 1;
+  wb.rank = 0;
+  fft_pass<true, ONED, false>(wb, sr, 0, L.psrow, true, local_bar);
+  if constexpr (!ONED) fft_pass<false, false, false>(wb, sc, 0, L.pscol, true, local_bar);
+
+  float* out = L.out + (size_t)(L.img0 + img) * L.out_stride + (size_t)t.out_ch * L.out_nr * L.out_nc;
+  for (int e = threadIdx.x; e < L.out_nr * L.out_nc; e += blockDim.x) {
+    const int p = e / L.out_nc + L.out_r0, q = e % L.out_nc + L.out_c0;
+    const float2* bp = ONED ? B + (q + (q >> 4)) : B + (size_t)p * L.ldb + q;
+    out[e] = bp->x;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct Group {
+  CascadeLaunch L;       // pointers filled at launch
+  std::vector<Task> tasks;
+  size_t task_off = 0;   // offset into the device task array
+  size_t smem = 0;
+  bool oned = false;
+  int level = 0;         // 0: input stage, 1: order 1, 2: order 2
+};
+
+int odd_pitch(int n) { return (n % 2 == 0) ? n + 1 : n; }
+int swz_len(int n) { return n + (n >> 4) + 1; }
+
+}  // namespace
+
+struct DeviceState {
+  Task* tasks = nullptr;
+  float2* tw = nullptr;
+};
+
+struct CascadePlan {
+  // geometry
+  bool oned = false;
+  int M = 0, N = 0, J = 0, L = 0, max_order = 2, pre_pad = 0;
+  int Mp = 0, Np = 0;
+  int channels = 0, out_nr = 0, out_nc = 0;
+  int img_M = 0, img_N = 0, pad_t = 0, pad_l = 0;
+  std::vector<int> filter_rows, filter_cols;  // expected filter shapes, by index
+  long long u0_elems = 0;                     // per image
+  long long u1_elems = 0;                     // per image
+  int chunk = 0;
+  std::vector<Group> groups;
+  std::vector<Task> all_tasks;
+  TwiddleBank tw;
+  std::mutex mu;                     // guards `dev`
+  std::map<int, DeviceState> dev;    // task and twiddle tables, per device
+  ~CascadePlan() {
+    int cur = 0;
+    const bool have = cudaGetDevice(&cur) == cudaSuccess;
+    for (auto& kv : dev) {
+      if (cudaSetDevice(kv.first) != cudaSuccess) continue;
+      cudaFree(kv.second.tasks);
+      cudaFree(kv.second.tw);
+    }
+    if (have) cudaSetDevice(cur);
+    cudaGetLastError();
+  }
+};
+
+// Host-side finalisation: task offsets into one concatenated table.
+static int finalize_groups(CascadePlan* P) {
+  size_t total = 0;
+  for (auto& g : P->groups) {
+    g.task_off = total;
+    total += g.tasks.size();
+  }
+  P->all_tasks.clear();
+  for (auto& g : P->groups) P->all_tasks.insert(P->all_tasks.end(), g.tasks.begin(), g.tasks.end());
+  return KYM_OK;
+}
+
+// Upload the task and twiddle tables to the current device on first use.
+static const DeviceState* device_state(CascadePlan* P) {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(P->mu);
+  auto it = P->dev.find(d);
+  if (it != P->dev.end()) return &it->second;
+  DeviceState s;
+  const size_t nt = P->all_tasks.size(), nw = P->tw.host().size();
+  if (cudaMalloc(&s.tasks, std::max<size_t>(nt, 1) * sizeof(Task)) != cudaSuccess) return nullptr;
+  if (cudaMalloc(&s.tw, std::max<size_t>(nw, 1) * sizeof(float2)) != cudaSuccess) {
+    cudaFree(s.tasks);
+    return nullptr;
+  }
+  if ((nt && cudaMemcpy(s.tasks, P->all_tasks.data(), nt * sizeof(Task), cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (nw && cudaMemcpy(s.tw, P->tw.host().data(), nw * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)) {
+    cudaFree(s.tasks);
+    cudaFree(s.tw);
+    return nullptr;
+  }
+  return &(P->dev[d] = s);
+}
+
+// Geometry of one group: work size (mr, mc), fold from the source, low-pass
+// size.  Chooses the cluster size and shared-memory layout.
+static int make_group(CascadePlan* P, Group& g, int mr, int mc, int kr, int kc, int sr, int sc, bool modulus,
+                      bool src_image) {
+  CascadeLaunch& L = g.L;
+  std::memset(&L, 0, sizeof(L));
+  g.oned = P->oned;
+  L.mr = mr;
+  L.mc = mc;
+  L.kr = kr;
+  L.kc = kc;
+  L.sr = sr;
+  L.sc = sc;
+  L.modulus = modulus ? 1 : 0;
+  L.src_image = src_image ? 1 : 0;
+  if (!make_fft_plan(mc, &L.prow, kThreads) || !make_fft_plan(mr, &L.pcol, kThreads) ||
+      !make_fft_plan(sc, &L.psrow, kThreads) || !make_fft_plan(sr, &L.pscol, kThreads))
+    return KYM_ERR_UNSUPPORTED;
+  P->tw.add(mc);
+  P->tw.add(mr);
+  P->tw.add(sc);
+  P->tw.add(sr);
+  const size_t max_smem = max_dynamic_smem();
+  if (P->oned) {
+    L.ld = swz_len(mc);
+    L.ldb = swz_len(sc);
+    L.cluster = 1;
+    L.rows_local = 1;
+    g.smem = ((size_t)L.ld + L.ldb) * sizeof(float2);
+    if (g.smem > max_smem) return KYM_ERR_UNSUPPORTED;
+  } else {
+    L.ld = odd_pitch(mc);
+    L.ldb = odd_pitch(sc);
+    int C = 0;
+    for (int c : {1, 2, 4, 8}) {
+      if (mr % c || mc % c) continue;
+      size_t s = ((size_t)(mr / c) * L.ld + (size_t)sr * L.ldb) * sizeof(float2);
+      if (c > 1) s += (size_t)mr * sizeof(void*);
+      if (s <= max_smem) {
+        C = c;
+        g.smem = s;
+        break;
+      }
+    }
+    if (!C) return KYM_ERR_UNSUPPORTED;
+    L.cluster = C;
+    L.rows_local = mr / C;
+  }
+  L.load_scale = src_image ? 1.f : (float)(1.0 / ((double)kr * kc) / (modulus ? (double)mr * mc : 1.0));
+  L.s_scale = (float)(1.0 / ((double)(mr / sr) * (mc / sc)) / ((double)sr * sc));
+  return KYM_OK;
+}
+
+template <bool CL, bool ONED>
+static cudaError_t launch_group(const Group& g, const CascadeLaunch& L, const FilterTable& F, int nimg,
+                                cudaStream_t stream) {
+  auto kern = cascade_kernel<CL, ONED>;
+  static int configured_device = -1;  // opt into the largest dynamic smem once per device
+  int d = 0;
+  cudaGetDevice(&d);
+  if (configured_device != d) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)max_dynamic_smem());
+    if (e != cudaSuccess) return e;
+    configured_device = d;
+  }
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(L.ntasks * L.cluster, nimg, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = g.smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  cfg.attrs = attr;
+  cfg.numAttrs = 0;
+  if (CL) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = L.cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, kern, L, F);
+}
+
+static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
+                    int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
+                    float* group_ms = nullptr, int max_groups = 0) {
+  if (!P || !x || !out || batch < 0) return KYM_ERR_INVALID;
+  if (batch == 0) return KYM_OK;
+  if (nfilters != (int)P->filter_rows.size() || nfilters > kMaxFilters) return KYM_ERR_INVALID;
+  FilterTable F;
+  std::memset(&F, 0, sizeof(F));
+  for (int i = 0; i < nfilters; ++i) {
+    if (!filters[i]) return KYM_ERR_INVALID;
+    F.f[i] = filters[i];
+  }
+  const int chunk = std::min(batch, P->chunk);
+  const size_t need = ((size_t)batch * P->u0_elems + (size_t)chunk * P->u1_elems) * sizeof(float2);
+  if (!workspace || ws_bytes < need) return KYM_ERR_WORKSPACE;
+  const DeviceState* ds = device_state(P);
+  if (!ds) return KYM_ERR_CUDA;
+  float2* u0 = static_cast<float2*>(workspace);
+  float2* u1 = u0 + (size_t)batch * P->u0_elems;
+  const long long x_stride = (long long)P->img_M * P->img_N;
+  const long long out_stride = (long long)P->channels * P->out_nr * P->out_nc;
+  cudaError_t err = cudaSuccess;
+  // optional timing: one event pair around every launch of every group
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> evs;
+  const bool timed = group_ms && max_groups > 0;
+  if (timed)
+    for (int i = 0; i < max_groups; ++i) group_ms[i] = 0.f;
+  for (int c0 = 0; c0 < batch; c0 += chunk) {
+    const int nimg = std::min(chunk, batch - c0);
+    for (size_t gi = 0; gi < P->groups.size(); ++gi) {
+      const Group& g = P->groups[gi];
+      if (g.level == 0 && c0 != 0) continue;  // the input stage runs once over the batch
+      CascadeLaunch L = g.L;
+      L.tasks = ds->tasks + g.task_off;
+      L.ntasks = (int)g.tasks.size();
+      L.prow.tw = ds->tw + P->tw.offset(L.prow.n);
+      L.pcol.tw = ds->tw + P->tw.offset(L.pcol.n);
+      L.psrow.tw = ds->tw + P->tw.offset(L.psrow.n);
+      L.pscol.tw = ds->tw + P->tw.offset(L.pscol.n);
+      L.x = x;
+      L.x_stride = x_stride;
+      L.out = out;
+      L.out_stride = out_stride;
+      int n = nimg;
+      if (g.level == 0) {
+        n = batch;
+        L.img0 = 0;
+        L.dst = u0;
+        L.dst_stride = P->u0_elems;
+      } else if (g.level == 1) {
+        L.img0 = c0;
+        L.src = u0 + (size_t)c0 * P->u0_elems;
+        L.src_stride = P->u0_elems;
+        L.dst = u1;
+        L.dst_stride = P->u1_elems;
+      } else {
+        L.img0 = c0;
+        L.src = u1;
+        L.src_stride = P->u1_elems;
+      }
+      // grid.y is limited to 65535 images per launch
+      for (int i0 = 0; i0 < n; i0 += 65535) {
+        CascadeLaunch Li = L;
+        const int ni = std::min(65535, n - i0);
+        Li.img0 = L.img0 + i0;
+        if (Li.src) Li.src = L.src + (size_t)i0 * L.src_stride;
+        if (Li.dst) Li.dst = L.dst + (size_t)i0 * L.dst_stride;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (timed && (int)gi < max_groups) {
+          cudaEventCreate(&e0);
+          cudaEventCreate(&e1);
+          cudaEventRecord(e0, stream);
+        }
+        if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
+        else if (Li.cluster > 1) err = launch_group<true, false>(g, Li, F, ni, stream);
+        else err = launch_group<false, false>(g, Li, F, ni, stream);
+        if (e0) {
+          cudaEventRecord(e1, stream);
+          evs.push_back({(int)gi, {e0, e1}});
+        }
+        if (err != cudaSuccess) {
+          for (auto& e : evs) {
+            cudaEventDestroy(e.second.first);
+            cudaEventDestroy(e.second.second);
+          }
+          return KYM_ERR_CUDA;
+        }
+      }
+    }
+  }
+  if (timed) {
+    if (cudaStreamSynchronize(stream) != cudaSuccess) err = cudaErrorUnknown;
+    for (auto& e : evs) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, e.second.first, e.second.second) == cudaSuccess) group_ms[e.first] += ms;
+      cudaEventDestroy(e.second.first);
+      cudaEventDestroy(e.second.second);
+    }
+    if (err != cudaSuccess) return KYM_ERR_CUDA;
+  }
+  return KYM_OK;
+}
+
+static void set_default_chunk(CascadePlan* P) {
+  const double budget = 64.0 * 1024 * 1024;  // keep parent spectra L2-resident
+  long long c = P->u1_elems ? (long long)(budget / (P->u1_elems * sizeof(float2))) : 1 << 20;
+  P->chunk = (int)std::max<long long>(1, std::min<long long>(c, 1 << 20));
+}
+
+}  // namespace kym
+
+using kym::CascadePlan;
+
+// ---------------------------------------------------------------------------
+// 2-D plan
+// ---------------------------------------------------------------------------
+struct kym_s2d_plan {
+  CascadePlan p;
+};
+
+extern "C" int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, int pre_pad, kym_s2d_plan** out) {
+  using namespace kym;
+  if (!out) return KYM_ERR_INVALID;
+  *out = nullptr;
+  if (M < 1 || N < 1 || J < 0 || L < 1 || max_order < 1 || max_order > 2) return KYM_ERR_INVALID;
+  if ((1 << J) > M || (1 << J) > N) return KYM_ERR_INVALID;
+  auto* h = new (std::nothrow) kym_s2d_plan;
+  if (!h) return KYM_ERR_CUDA;
+  CascadePlan* P = &h->p;
+  P->M = M;
+  P->N = N;
+  P->J = J;
+  P->L = L;
+  P->max_order = max_order;
+  P->pre_pad = pre_pad;
+  const int k = 1 << J;
+  P->Mp = ((M + k) / k + 1) * k;
+  P->Np = ((N + k) / k + 1) * k;
+  P->img_M = pre_pad ? P->Mp : M;
+  P->img_N = pre_pad ? P->Np : N;
+  P->pad_t = pre_pad ? 0 : (P->Mp - M) / 2;
+  P->pad_l = pre_pad ? 0 : (P->Np - N) / 2;
+  const int sr = P->Mp / k, sc = P->Np / k;
+  P->out_nr = sr - 2;
+  P->out_nc = sc - 2;
+  // filter index layout: phi levels 0..J-1, then every psi's levels
+  // (the order of the reference's registered buffers tensor0..tensorK)
+  for (int r = 0; r < J; ++r) {
+    P->filter_rows.push_back(P->Mp >> r);
+    P->filter_cols.push_back(P->Np >> r);
+  }
+  std::vector<int> psi_first(J * L);
+  for (int j = 0; j < J; ++j)
+    for (int t = 0; t < L; ++t) {
+      psi_first[j * L + t] = (int)P->filter_rows.size();
+      const int nlev = std::min(j + 1, std::max(J - 1, 1));
+      for (int r = 0; r < nlev; ++r) {
+        P->filter_rows.push_back(P->Mp >> r);
+        P->filter_cols.push_back(P->Np >> r);
+      }
+    }
+  if ((int)P->filter_rows.size() > kMaxFilters) {
+    delete h;
+    return KYM_ERR_UNSUPPORTED;
+  }
+  P->u0_elems = (long long)P->Mp * P->Np;
+  std::vector<long long> u1_off(J * L, -1);
+  long long u1 = 0;
+  if (max_order >= 2)
+    for (int n1 = 0; n1 < J * L; ++n1) {
+      const int j1 = n1 / L;
+      if (j1 < J - 1) {
+        u1_off[n1] = u1;
+        u1 += (long long)(P->Mp >> j1) * (P->Np >> j1);
+      }
+    }
+  P->u1_elems = u1;
+  int rc = KYM_OK;
+  // input stage
+  {
+    Group g;
+    rc = make_group(P, g, P->Mp, P->Np, 1, 1, sr, sc, false, true);
+    if (rc) goto fail;
+    g.level = 0;
+    g.L.out_r0 = 1;
+    g.L.out_c0 = 1;
+    g.L.out_nr = P->out_nr;
+    g.L.out_nc = P->out_nc;
+    g.L.img_M = P->img_M;
+    g.L.img_N = P->img_N;
+    g.L.pad_t = P->pad_t;
+    g.L.pad_l = P->pad_l;
+    g.tasks.push_back(Task{0, 0, -1, 0, 0, 0});
+    P->groups.push_back(g);
+  }
+  // order 1, one launch per scale
+  for (int j1 = 0; j1 < J; ++j1) {
+    Group g;
+    rc = make_group(P, g, P->Mp >> j1, P->Np >> j1, 1 << j1, 1 << j1, sr, sc, true, false);
+    if (rc) goto fail;
+    g.level = 1;
+    g.L.out_r0 = 1;
+    g.L.out_c0 = 1;
+    g.L.out_nr = P->out_nr;
+    g.L.out_nc = P->out_nc;
+    for (int t = 0; t < L; ++t) {
+      const int n1 = j1 * L + t;
+      g.tasks.push_back(Task{0, u1_off[n1], psi_first[n1], j1, 1 + n1, 0});
+    }
+    P->groups.push_back(g);
+  }
+  // order 2, one launch per (j1, j2)
+  if (max_order >= 2) {
+    int ch = 1 + J * L;
+    std::map<std::pair<int, int>, Group> byscale;
+    std::vector<std::pair<int, int>> order;
+    for (int n1 = 0; n1 < J * L; ++n1) {
+      const int j1 = n1 / L;
+      for (int n2 = 0; n2 < J * L; ++n2) {
+        const int j2 = n2 / L;
+        if (j2 <= j1) continue;
+        auto key = std::make_pair(j1, j2);
+        if (!byscale.count(key)) {
+          Group g;
+          rc = make_group(P, g, P->Mp >> j2, P->Np >> j2, 1 << (j2 - j1), 1 << (j2 - j1), sr, sc, true, false);
+          if (rc) goto fail;
+          g.level = 2;
+          g.L.out_r0 = 1;
+          g.L.out_c0 = 1;
+          g.L.out_nr = P->out_nr;
+          g.L.out_nc = P->out_nc;
+          byscale[key] = g;
+          order.push_back(key);
+        }
+        byscale[key].tasks.push_back(Task{u1_off[n1], -1, psi_first[n2] + j1, j2, ch++, 0});
+      }
+    }
+    for (auto& key : order) P->groups.push_back(byscale[key]);
+    P->channels = ch;
+  } else {
+    P->channels = 1 + J * L;
+  }
+  for (auto& g : P->groups) g.L.out_channels = P->channels;
+  rc = finalize_groups(P);
+  if (rc) goto fail;
+  set_default_chunk(P);
+  *out = h;
+  return KYM_OK;
+fail:
+  delete h;
+  return rc;
+}
+
+extern "C" int kym_s2d_plan_destroy(kym_s2d_plan* plan) {
+  delete plan;
+  return KYM_OK;
+}
+
+extern "C" int kym_s2d_plan_info(const kym_s2d_plan* plan, int* M_padded, int* N_padded, int* channels,
+                                 int* out_rows, int* out_cols, int* n_filters) {
+  if (!plan) return KYM_ERR_INVALID;
+  const CascadePlan& P = plan->p;
+  if (M_padded) *M_padded = P.Mp;
+  if (N_padded) *N_padded = P.Np;
+  if (channels) *channels = P.channels;
+  if (out_rows) *out_rows = P.out_nr;
+  if (out_cols) *out_cols = P.out_nc;
+  if (n_filters) *n_filters = (int)P.filter_rows.size();
+  return KYM_OK;
+}
+
+extern "C" int kym_s2d_filter_shape(const kym_s2d_plan* plan, int index, int* rows, int* cols) {
+  if (!plan || index < 0 || index >= (int)plan->p.filter_rows.size()) return KYM_ERR_INVALID;
+  if (rows) *rows = plan->p.filter_rows[index];
+  if (cols) *cols = plan->p.filter_cols[index];
+  return KYM_OK;
+}
+
+extern "C" int kym_s2d_set_chunk(kym_s2d_plan* plan, int chunk) {
+  if (!plan || chunk < 1) return KYM_ERR_INVALID;
+  plan->p.chunk = chunk;
+  return KYM_OK;
+}
+
+extern "C" int kym_s2d_get_chunk(const kym_s2d_plan* plan) { return plan ? plan->p.chunk : -1; }
+
+extern "C" int kym_s2d_group_count(const kym_s2d_plan* plan) {
+  return plan ? (int)plan->p.groups.size() : -1;
+}
+
+extern "C" int kym_s2d_group_info(const kym_s2d_plan* plan, int group, int* level, int* ntasks, int* rows,
+                                  int* cols, int* fold, int* cluster) {
+  if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return KYM_ERR_INVALID;
+  const kym::Group& g = plan->p.groups[group];
+  if (level) *level = g.level;
+  if (ntasks) *ntasks = (int)g.tasks.size();
+  if (rows) *rows = g.L.mr;
+  if (cols) *cols = g.L.mc;
+  if (fold) *fold = g.L.kc;
+  if (cluster) *cluster = g.L.cluster;
+  return KYM_OK;
+}
+
+extern "C" int kym_s2d_forward_timed(const kym_s2d_plan* plan, const float* x, float* out, int batch,
+                                     const float* const* filters, int n_filters, void* workspace,
+                                     size_t workspace_bytes, void* stream, float* group_ms, int max_groups) {
+  if (!plan || !group_ms || max_groups < 1) return KYM_ERR_INVALID;
+  return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
+                       workspace_bytes, static_cast<cudaStream_t>(stream), group_ms, max_groups);
+}
+
+extern "C" size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch) {
+  if (!plan || batch < 0) return 0;
+  const CascadePlan& P = plan->p;
+  const int chunk = std::min(batch, P.chunk);
+  return ((size_t)batch * P.u0_elems + (size_t)chunk * P.u1_elems) * sizeof(float2);
+}
+
+extern "C" int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch,
+                               const float* const* filters, int n_filters, void* workspace,
+                               size_t workspace_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
+                       workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+// ---------------------------------------------------------------------------
+// 1-D plan
+// ---------------------------------------------------------------------------
+struct kym_s1d_plan {
+  CascadePlan p;
+};
+
+extern "C" int kym_s1d_plan_create(int N_padded, int N_input, int pad_left, int log2_stride, int max_order,
+                                   int n_psi1, const int* psi1_j, const int* psi1_nlevels, int n_psi2,
+                                   const int* psi2_j, const int* psi2_nlevels, int n_phi_levels, int out_start,
+                                   int out_end, kym_s1d_plan** out) {
+  using namespace kym;
+  if (!out) return KYM_ERR_INVALID;
+  *out = nullptr;
+  if (N_padded < 2 || (N_padded & (N_padded - 1)) || N_input < 1 || log2_stride < 0 ||
+      (1 << log2_stride) > N_padded || max_order < 1 || max_order > 2 || n_psi1 < 0 || n_psi2 < 0 ||
+      (n_psi1 && (!psi1_j || !psi1_nlevels)) || (n_psi2 && (!psi2_j || !psi2_nlevels)) || n_phi_levels < 1 ||
+      out_start < 0 || out_end <= out_start || out_end > (N_padded >> log2_stride))
+    return KYM_ERR_INVALID;
+  auto* h = new (std::nothrow) kym_s1d_plan;
+  if (!h) return KYM_ERR_CUDA;
+  CascadePlan* P = &h->p;
+  P->oned = true;
+  P->Mp = 1;
+  P->Np = N_padded;
+  P->img_M = 1;
+  P->img_N = N_input;
+  P->pad_t = 0;
+  P->pad_l = pad_left;
+  P->out_nr = 1;
+  P->out_nc = out_end - out_start;
+  const int S = N_padded >> log2_stride;
+  int rc = KYM_OK;
+  // filter index layout: phi levels, psi1 levels, psi2 levels
+  std::vector<int> phi_idx, psi1_first, psi2_first;
+  for (int l = 0; l < n_phi_levels; ++l) {
+    phi_idx.push_back((int)P->filter_rows.size());
+    P->filter_rows.push_back(1);
+    P->filter_cols.push_back(N_padded >> l);
+  }
+  for (int n = 0; n < n_psi1; ++n) {
+    psi1_first.push_back((int)P->filter_rows.size());
+    for (int l = 0; l < psi1_nlevels[n]; ++l) {
+      P->filter_rows.push_back(1);
+      P->filter_cols.push_back(N_padded >> l);
+    }
+  }
+  for (int n = 0; n < n_psi2; ++n) {
+    psi2_first.push_back((int)P->filter_rows.size());
+    for (int l = 0; l < psi2_nlevels[n]; ++l) {
+      P->filter_rows.push_back(1);
+      P->filter_cols.push_back(N_padded >> l);
+    }
+  }
+  if ((int)P->filter_rows.size() > kMaxFilters) {
+    delete h;
+    return KYM_ERR_UNSUPPORTED;
+  }
+  auto mk = [&](Group& g, int m, int kfold, int level, bool modulus, bool image) -> int {
+    int r = make_group(P, g, 1, m, 1, kfold, 1, S, modulus, image);
+    if (r) return r;
+    g.level = level;
+    g.L.out_r0 = 0;
+    g.L.out_c0 = out_start;
+    g.L.out_nr = 1;
+    g.L.out_nc = P->out_nc;
+    g.L.img_M = 1;
+    g.L.img_N = N_input;
+    g.L.pad_t = 0;
+    g.L.pad_l = pad_left;
+    return KYM_OK;
+  };
+  P->u0_elems = N_padded;
+  // parents that have children, by (k1) resolution
+  std::vector<long long> u1_off(n_psi1, -1);
+  long long u1 = 0;
+  const bool second = max_order >= 2 && n_psi2 > 0;
+  int ch = 0;
+  std::map<std::tuple<int, int, int>, Group> groups;  // (level, m, fold) -> group
+  std::vector<std::tuple<int, int, int>> order;
+  auto group_for = [&](int level, int m, int kfold, bool modulus, bool image) -> Group* {
+    auto key = std::make_tuple(level, m, kfold);
+    if (!groups.count(key)) {
+      Group g;
+      if (mk(g, m, kfold, level, modulus, image)) return nullptr;
+      groups[key] = g;
+      order.push_back(key);
+    }
+    return &groups[key];
+  };
+  {
+    Group* g = group_for(0, N_padded, 1, false, true);
+    if (!g) { rc = KYM_ERR_UNSUPPORTED; goto fail; }
+    // phi level 0 with the input stage; fold factor 2^log2_stride for S
+    g->tasks.push_back(Task{0, 0, -1, phi_idx[0], ch++, 0});
+  }
+  for (int n1 = 0; n1 < n_psi1; ++n1) {
+    const int j1 = psi1_j[n1];
+    const int k1 = std::min(j1, log2_stride);
+    bool has_child = false;
+    if (second)
+      for (int n2 = 0; n2 < n_psi2; ++n2) has_child |= psi2_j[n2] > j1;
+    if (has_child) {
+      u1_off[n1] = u1;
+      u1 += N_padded >> k1;
+    }
+    if (k1 >= n_phi_levels) { rc = KYM_ERR_INVALID; goto fail; }
+    Group* g = group_for(1, N_padded >> k1, 1 << k1, true, false);
+    if (!g) { rc = KYM_ERR_UNSUPPORTED; goto fail; }
+    g->tasks.push_back(Task{0, u1_off[n1], psi1_first[n1], phi_idx[k1], ch++, 0});
+  }
+  if (second) {
+    for (int n1 = 0; n1 < n_psi1; ++n1) {
+      const int j1 = psi1_j[n1];
+      const int k1 = std::min(j1, log2_stride);
+      for (int n2 = 0; n2 < n_psi2; ++n2) {
+        const int j2 = psi2_j[n2];
+        if (j2 <= j1) continue;
+        const int sub2 = std::min(j2, log2_stride);
+        const int k2 = std::max(sub2 - k1, 0);
+        if (k1 >= psi2_nlevels[n2] || k1 + k2 >= n_phi_levels) { rc = KYM_ERR_INVALID; goto fail; }
+        Group* g = group_for(2, N_padded >> (k1 + k2), 1 << k2, true, false);
+        if (!g) { rc = KYM_ERR_UNSUPPORTED; goto fail; }
+        g->tasks.push_back(Task{u1_off[n1], -1, psi2_first[n2] + k1, phi_idx[k1 + k2], ch++, 0});
+      }
+    }
+  }
+  for (auto& key : order) P->groups.push_back(groups[key]);
+  P->channels = ch;
+  P->u1_elems = u1;
+  for (auto& g : P->groups) g.L.out_channels = P->channels;
+  rc = finalize_groups(P);
+  if (rc) goto fail;
+  set_default_chunk(P);
+  *out = h;
+  return KYM_OK;
+fail:
+  delete h;
+  return rc;
+}
+
+extern "C" int kym_s1d_plan_destroy(kym_s1d_plan* plan) {
+  delete plan;
+  return KYM_OK;
+}
+
+extern "C" int kym_s1d_plan_info(const kym_s1d_plan* plan, int* channels, int* out_len, int* n_filters) {
+  if (!plan) return KYM_ERR_INVALID;
+  if (channels) *channels = plan->p.channels;
+  if (out_len) *out_len = plan->p.out_nc;
+  if (n_filters) *n_filters = (int)plan->p.filter_rows.size();
+  return KYM_OK;
+}
+
+extern "C" size_t kym_s1d_workspace_bytes(const kym_s1d_plan* plan, int batch) {
+  if (!plan || batch < 0) return 0;
+  const CascadePlan& P = plan->p;
+  const int chunk = std::min(batch, P.chunk);
+  return ((size_t)batch * P.u0_elems + (size_t)chunk * P.u1_elems) * sizeof(float2);
+}
+
+extern "C" int kym_s1d_set_chunk(kym_s1d_plan* plan, int chunk) {
+  if (!plan || chunk < 1) return KYM_ERR_INVALID;
+  plan->p.chunk = chunk;
+  return KYM_OK;
+}
+
+extern "C" int kym_s1d_forward(const kym_s1d_plan* plan, const float* x, float* out, int batch,
+                               const float* const* filters, int n_filters, void* workspace,
+                               size_t workspace_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
+                       workspace_bytes, static_cast<cudaStream_t>(stream));
+}

@@ -1,0 +1,62 @@
+// Fused scattering cascade: one CTA (or one thread-block cluster) runs one
+// scattering path of one image end to end in shared memory.
+//
+// A task reads a source (the real input image with reflect padding, or a
+// spectrum in global memory), forms   A = fold_{kr x kc}(src * psi)
+// (the cdgmm of kymatio/backend/torch_backend.py:147-219 fused with the
+// periodisation of kymatio/scattering2d/backend/torch_backend.py:92-129),
+// optionally runs  A <- FFT2(|IFFT2(A)|)  (kymatio/scattering2d/core/
+// scattering2d.py:37-39), optionally stores A as the parent spectrum of the
+// next order, and finishes with the low-pass branch
+//   S = unpad(Re IFFT2(fold_{ksr x ksc}(A * phi)))
+// (scattering2d.py:42-46) written straight into its output channel.  The 1-D
+// cascade (kymatio/scattering1d/core/scattering1d.py:40-107) is the same
+// program on a single row.
+#pragma once
+#include "fft_engine.cuh"
+
+namespace kym {
+
+constexpr int kMaxFilters = 1024;
+
+struct FilterTable {
+  const float* f[kMaxFilters];
+};
+
+struct Task {
+  long long src_off;  // complex-element offset of the source spectrum within one image's block
+  long long dst_off;  // offset of the stored spectrum, -1 if none
+  int psi;            // filter index multiplied before the fold, -1 if none
+  int phi;            // low-pass filter index
+  int out_ch;         // output channel
+  int pad_;
+};
+
+struct CascadeLaunch {
+  int mr, mc, kr, kc;     // work size and load-fold factors (source is kr*mr x kc*mc)
+  int ld;                 // shared-memory pitch of the work array (complex elements)
+  int sr, sc, ldb;        // low-pass output size and its pitch
+  int modulus;            // 1: IFFT2, modulus, FFT2
+  int src_image;          // 1: source is the real input image
+  int cluster;            // CTAs per task
+  int rows_local;         // mr / cluster
+  FftPlan prow, pcol, psrow, pscol;
+  float load_scale, s_scale;
+  int out_r0, out_c0, out_nr, out_nc, out_channels;
+  // image source (reflect padding folded into the load)
+  const float* x;
+  int img_M, img_N, pad_t, pad_l;
+  long long x_stride;
+  // spectra
+  const float2* src;
+  long long src_stride;
+  float2* dst;
+  long long dst_stride;
+  float* out;
+  long long out_stride;
+  const Task* tasks;
+  int ntasks;
+  int img0;  // first image of this chunk (for x/out offsets)
+};
+
+}  // namespace kym

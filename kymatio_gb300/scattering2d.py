@@ -1,0 +1,183 @@
+"""Scattering2D: drop-in for kymatio's ScatteringTorch2D on one GB300.
+
+Constructor, registered buffers (``tensor0..tensorK``, shape (m, n, 1), in
+the order of kymatio/scattering2d/frontend/torch_frontend.py:28-43), input
+validation and error messages (:72-111, kymatio/frontend/torch_frontend.py:
+13-18, kymatio/backend/torch_backend.py:102-107) and output layout
+(S0, S1 over n1, S2 over (n1, n2) with j2 > j1, n1-major; or a list of
+dicts with 'coef', 'j', 'n', 'theta') follow the reference.  The transform
+itself is one fused CUDA cascade (kym_s2d_forward) on the tensor's device
+and torch's current stream; CPU tensors are rejected, there is no fallback.
+"""
+import torch
+import torch.nn as nn
+
+from . import _lib
+from .filter_bank import filter_bank_2d, padded_size_2d
+
+
+class Scattering2D(nn.Module):
+    """2-D scattering transform (Mallat) with Morlet wavelets.
+
+    Parameters follow kymatio.torch.Scattering2D: J (log2 scale), shape (M, N),
+    L (orientations, default 8), max_order (1 or 2), pre_pad (input already
+    padded to the padded size), backend (accepted for signature
+    compatibility; the engine is always the GB300 cascade), out_type
+    ('array' or 'list').
+    """
+
+    def __init__(self, J, shape, L=8, max_order=2, pre_pad=False, backend='torch', out_type='array'):
+        super().__init__()
+        self.frontend_name = 'torch'
+        if backend is not None and not isinstance(backend, str) and \
+                not str(getattr(backend, 'name', '')).startswith('torch'):
+            raise ImportError('The backend ' + str(getattr(backend, 'name', backend)) +
+                              ' is not supported by the frontend torch.')
+        self.backend = backend
+        self.J, self.L, self.max_order = int(J), int(L), int(max_order)
+        self.pre_pad, self.out_type = pre_pad, out_type
+        self.shape = tuple(int(s) for s in shape)
+        M, N = self.shape
+        if 2 ** self.J > M or 2 ** self.J > N:
+            raise RuntimeError('The smallest dimension should be larger than 2^J.')
+        self._M_padded, self._N_padded = padded_size_2d(M, N, self.J)
+        self.pad_size = [(self._M_padded - M) // 2, (self._M_padded - M + 1) // 2,
+                         (self._N_padded - N) // 2, (self._N_padded - N + 1) // 2]
+        phi, psi = filter_bank_2d(self._M_padded, self._N_padded, self.J, self.L)
+        self.phi = {'levels': list(phi), 'j': self.J}
+        self.psi = [{'levels': list(p['levels']), 'j': p['j'], 'theta': p['theta']} for p in psi]
+        n = 0
+        for lv in self.phi['levels']:
+            self.register_buffer('tensor' + str(n), torch.from_numpy(lv.copy()).unsqueeze(-1))
+            n += 1
+        for p in self.psi:
+            for lv in p['levels']:
+                self.register_buffer('tensor' + str(n), torch.from_numpy(lv.copy()).unsqueeze(-1))
+                n += 1
+        self._n_filters = n
+        self._plan = None
+        self._ptr_cache = (None, None)
+        self._meta = self._path_meta()
+
+    # -- plan ---------------------------------------------------------------
+    def _get_plan(self):
+        if self._plan is None:
+            lib = _lib.load()
+            h = _lib._vp()
+            _lib.check(lib.kym_s2d_plan_create(self.shape[0], self.shape[1], self.J, self.L, self.max_order,
+                                               int(bool(self.pre_pad)), _lib.ctypes.byref(h)),
+                       'kym_s2d_plan_create')
+            self._plan = _Plan(lib, h.value, lib.kym_s2d_plan_destroy)
+            ints = [_lib.ctypes.c_int() for _ in range(6)]
+            _lib.check(lib.kym_s2d_plan_info(self._plan.h, *[_lib.ctypes.byref(i) for i in ints]),
+                       'kym_s2d_plan_info')
+            self._channels, self._out_hw = ints[2].value, (ints[3].value, ints[4].value)
+            if ints[5].value != self._n_filters:
+                raise RuntimeError('filter bank layout mismatch')
+        return self._plan
+
+    def set_chunk(self, chunk):
+        """Images per order-2 pass (autotuned); bounds the workspace."""
+        _lib.check(_lib.load().kym_s2d_set_chunk(self._get_plan().h, int(chunk)), 'kym_s2d_set_chunk')
+
+    def _path_meta(self):
+        meta = [{'j': (), 'n': (), 'theta': ()}]
+        for n1, p in enumerate(self.psi):
+            meta.append({'j': (p['j'],), 'n': (n1,), 'theta': (p['theta'],)})
+        if self.max_order >= 2:
+            for n1, p1 in enumerate(self.psi):
+                for n2, p2 in enumerate(self.psi):
+                    if p2['j'] > p1['j']:
+                        meta.append({'j': (p1['j'], p2['j']), 'n': (n1, n2), 'theta': (p1['theta'], p2['theta'])})
+        return meta
+
+    def _filter_ptrs(self):
+        bufs = [getattr(self, 'tensor' + str(i)) for i in range(self._n_filters)]
+        key = tuple(b.data_ptr() for b in bufs)
+        if self._ptr_cache[0] != key:
+            for b in bufs:
+                if not b.is_cuda or b.dtype != torch.float32 or not b.is_contiguous():
+                    raise TypeError('The filters must be contiguous float32 CUDA tensors; call .cuda() on the '
+                                    'module (the GB300 engine runs on CUDA only).')
+            self._ptr_cache = (key, _lib.ptr_array(list(key)))
+        return self._ptr_cache[1]
+
+    # -- forward ------------------------------------------------------------
+    def forward(self, x):
+        if x is None:
+            raise TypeError('The input should be not empty.')
+        if torch.is_tensor(x) and not x.is_contiguous():
+            raise RuntimeError('Tensors must be contiguous.')
+        return self.scattering(x)
+
+    def scattering(self, input):
+        if not torch.is_tensor(input):
+            raise TypeError('The input should be a PyTorch Tensor.')
+        if len(input.shape) < 2:
+            raise RuntimeError('Input tensor must have at least two dimensions.')
+        if not input.is_contiguous():
+            raise RuntimeError('Tensor must be contiguous.')
+        if (input.shape[-1] != self.shape[-1] or input.shape[-2] != self.shape[-2]) and not self.pre_pad:
+            raise RuntimeError('Tensor must be of spatial size (%i,%i).' % (self.shape[0], self.shape[1]))
+        if (input.shape[-1] != self._N_padded or input.shape[-2] != self._M_padded) and self.pre_pad:
+            raise RuntimeError('Padded tensor must be of spatial size (%i,%i).' % (self._M_padded, self._N_padded))
+        if self.out_type not in ('array', 'list'):
+            raise RuntimeError("The out_type must be one of 'array' or 'list'.")
+        if not input.is_cuda:
+            raise TypeError('The input must be a CUDA tensor: the GB300 scattering engine runs on CUDA only.')
+        if input.dtype != torch.float32:
+            raise TypeError('The input must be float32 (got %s).' % input.dtype)
+        batch_shape = input.shape[:-2]
+        x = input.reshape((-1,) + tuple(input.shape[-2:]))
+        S = _Scattering2DFn.apply(x, self)
+        S = S.reshape(tuple(batch_shape) + tuple(S.shape[-3:]))
+        if self.out_type == 'array':
+            return S
+        return [dict(m, coef=S[..., c, :, :]) for c, m in enumerate(self._meta)]
+
+    def _forward_raw(self, x):
+        """(B, M, N) float32 CUDA -> (B, C, m, n) through kym_s2d_forward."""
+        plan = self._get_plan()
+        lib = _lib.load()
+        B = x.shape[0]
+        out = torch.empty((B, self._channels) + self._out_hw, dtype=torch.float32, device=x.device)
+        if B == 0:
+            return out
+        with torch.cuda.device(x.device):
+            ptrs = self._filter_ptrs()
+            ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, B)
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=x.device)
+            stream = torch.cuda.current_stream(x.device).cuda_stream
+            _lib.check(lib.kym_s2d_forward(plan.h, x.data_ptr(), out.data_ptr(), B, ptrs, self._n_filters,
+                                           ws.data_ptr(), ws_bytes, stream), 'kym_s2d_forward')
+        return out
+
+    def extra_repr(self):
+        return 'J={}, shape={}, L={}, max_order={}, pre_pad={}, out_type={!r}'.format(
+            self.J, self.shape, self.L, self.max_order, self.pre_pad, self.out_type)
+
+
+class _Plan:
+    """Owns a C plan handle."""
+
+    def __init__(self, lib, h, destroy):
+        self.h, self._destroy = h, destroy
+
+    def __del__(self):
+        try:
+            self._destroy(self.h)
+        except Exception:
+            pass
+
+
+class _Scattering2DFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, module):
+        ctx.module = module
+        ctx.save_for_backward(x)
+        return module._forward_raw(x)
+
+    @staticmethod
+    def backward(ctx, grad):
+        (x,) = ctx.saved_tensors
+        return ctx.module._backward_raw(x, grad.contiguous()), None

@@ -1,0 +1,116 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Run once in a container where the reference checkout is available:
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+
+It imports the reference's numpy frontends (the ``kymatio.numpy`` namespace
+is avoided because it pulls in the 3-D filter bank, whose scipy import fails
+on current scipy) and writes:
+
+* ``ref_test_data_2d.npz`` / ``ref_test_data_1d.npz`` -- the reference's own
+  golden vectors (tests/scattering2d/test_data_2d.npz,
+  tests/scattering1d/test_data_1d.npz) re-exported unchanged;
+* ``ref_cases_2d.npz`` -- seeded inputs and reference numpy FP64 outputs for
+  small 2-D configurations (odd, non-square, pre_pad, max_order=1, L=4, the
+  256x256 J=3 shape);
+* ``ref_cases_1d.npz`` -- the same for 1-D configurations (T local, global,
+  zero, stride, the 8192-sample J=6 Q=(8,1) T=64 shape);
+* ``ref_bank_2d.npz`` -- the full 40x40 J=2 filter bank and per-filter
+  checksums of the 272x272 J=3 bank.
+
+Nothing at test time reads the reference; the tests read these files.
+"""
+import io
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+CASES_2D = [
+    # name, J, (M, N), L, max_order, pre_pad, batch
+    ('j2_32', 2, (32, 32), 8, 2, False, 3),
+    ('j1_31', 1, (31, 31), 8, 2, False, 2),
+    ('j4_33', 4, (33, 33), 8, 2, False, 2),
+    ('j5_37x32', 5, (37, 32), 8, 2, False, 2),
+    ('j3_64x48', 3, (64, 48), 8, 2, False, 2),
+    ('j2_20x24_prepad', 2, (20, 24), 8, 2, True, 2),
+    ('j3_40_order1', 3, (40, 40), 8, 1, False, 2),
+    ('j2_24_L4', 2, (24, 24), 4, 2, False, 2),
+    ('j2_8', 2, (8, 8), 8, 2, False, 2),
+    ('j3_256', 3, (256, 256), 8, 2, False, 1),
+]
+
+CASES_1D = [
+    # name, kwargs, batch
+    ('j6_q8_t64_n8192', dict(J=6, shape=8192, Q=(8, 1), T=64), 2),
+    ('j4_q2_global_n300', dict(J=4, shape=300, Q=2, T='global'), 2),
+    ('j5_q4_t0_n1024', dict(J=5, shape=1024, Q=4, T=0, out_type='list'), 2),
+    ('j5_q3_stride4_n1000', dict(J=5, shape=1000, Q=3, stride=4), 2),
+    ('j6_q8_os1_n512', dict(J=6, shape=512, Q=8, oversampling=1), 2),
+    ('j3_q1_t8_n64_order1', dict(J=3, shape=64, Q=1, T=8, max_order=1), 3),
+]
+
+
+def main(ref_root):
+    sys.path.insert(0, ref_root)
+    from kymatio.scattering2d.frontend.numpy_frontend import ScatteringNumPy2D
+    from kymatio.scattering1d.frontend.numpy_frontend import ScatteringNumPy1D
+
+    for src, dst in [('tests/scattering2d/test_data_2d.npz', 'ref_test_data_2d.npz'),
+                     ('tests/scattering1d/test_data_1d.npz', 'ref_test_data_1d.npz')]:
+        with open(os.path.join(ref_root, src), 'rb') as f:
+            data = np.load(io.BytesIO(f.read()))
+            np.savez_compressed(os.path.join(HERE, dst), **{k: data[k] for k in data.files})
+
+    out, meta = {}, []
+    for i, (name, J, shape, L, mo, pp, B) in enumerate(CASES_2D):
+        S = ScatteringNumPy2D(J, shape, L=L, max_order=mo, pre_pad=pp)
+        xs = (B, S._M_padded, S._N_padded) if pp else (B,) + shape
+        x = np.random.default_rng(100 + i).random(xs).astype(np.float32)
+        y = S(x.astype(np.float64))
+        out[name + '/x'] = x
+        out[name + '/S'] = y.astype(np.float32) if name == 'j3_256' else y
+        meta.append(dict(name=name, J=J, shape=list(shape), L=L, max_order=mo, pre_pad=pp))
+    out['meta'] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, 'ref_cases_2d.npz'), **out)
+
+    out, meta = {}, []
+    for i, (name, kw, B) in enumerate(CASES_1D):
+        S = ScatteringNumPy1D(**kw)
+        x = np.random.default_rng(200 + i).standard_normal((B, kw['shape'])).astype(np.float32)
+        y = S(x.astype(np.float64))
+        out[name + '/x'] = x
+        if isinstance(y, list):
+            for p in y:
+                out[name + '/S/' + ','.join(map(str, p['n']))] = p['coef']
+        else:
+            out[name + '/S'] = y
+        meta.append(dict(name=name, kwargs=kw))
+    out['meta'] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, 'ref_cases_1d.npz'), **out)
+
+    from kymatio.scattering2d.filter_bank import filter_bank
+    bank = filter_bank(40, 40, 2, 8)
+    out = {}
+    for r, lv in enumerate(bank['phi']['levels']):
+        out['phi/%d' % r] = lv
+    for n, p in enumerate(bank['psi']):
+        for r, lv in enumerate(p['levels']):
+            out['psi/%d/%d' % (n, r)] = lv
+    big = filter_bank(272, 272, 3, 8)
+    sums = []
+    for lv in big['phi']['levels']:
+        sums.append([lv.sum(dtype=np.float64), (lv.astype(np.float64) ** 2).sum(), lv[0, 0], lv[3, 5]])
+    for p in big['psi']:
+        for lv in p['levels']:
+            sums.append([lv.sum(dtype=np.float64), (lv.astype(np.float64) ** 2).sum(), lv[0, 0], lv[3, 5]])
+    out['big272/checksums'] = np.array(sums)
+    np.savez_compressed(os.path.join(HERE, 'ref_bank_2d.npz'), **out)
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')

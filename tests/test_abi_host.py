@@ -1,0 +1,92 @@
+"""Host-side checks of the C ABI library (no GPU needed): it loads, it exports
+every entry point include/kymatio_gb300.h declares, and its plans reproduce
+the reference geometry."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+
+def _declared():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, 'include')):
+        if f.endswith('.h'):
+            src = open(os.path.join(ROOT, 'include', f)).read()
+            src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+            names |= set(re.findall(r'\b(kym_\w+)\s*\(', src))
+    return names
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from kymatio_gb300 import _lib
+    return _lib.load(build_if_missing=True)
+
+
+def test_exports_every_declared_symbol(lib):
+    from kymatio_gb300 import _lib
+    declared = _declared()
+    assert declared, 'no declarations found'
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared == set(_lib.SIGNATURES), declared ^ set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize('M,N,J,L,mo,pp', [(256, 256, 3, 8, 2, 0), (32, 32, 2, 8, 2, 0), (128, 128, 4, 8, 2, 0),
+                                          (37, 32, 5, 8, 2, 0), (31, 31, 1, 8, 1, 0), (64, 48, 3, 8, 2, 1),
+                                          (24, 24, 2, 4, 2, 0), (256, 256, 4, 8, 2, 0)])
+def test_plan_geometry_2d(lib, M, N, J, L, mo, pp):
+    from oracle.scattering2d import Scattering2D as O
+    from kymatio_gb300 import _lib
+    h = _lib._vp()
+    assert lib.kym_s2d_plan_create(M, N, J, L, mo, pp, ctypes.byref(h)) == 0
+    v = [ctypes.c_int() for _ in range(6)]
+    assert lib.kym_s2d_plan_info(h, *[ctypes.byref(i) for i in v]) == 0
+    Mp, Np, C, orr, occ, nf = [i.value for i in v]
+    o = O.__new__(O)
+    from oracle.filters import compute_padding_2d
+    assert (Mp, Np) == compute_padding_2d(M, N, J)
+    c2 = L * L * J * (J - 1) // 2 if mo == 2 else 0
+    assert C == 1 + J * L + c2
+    assert (orr, occ) == (Mp // 2 ** J - 2, Np // 2 ** J - 2)
+    assert nf == J + L * sum(min(j + 1, max(J - 1, 1)) for j in range(J))
+    r, c = ctypes.c_int(), ctypes.c_int()
+    assert lib.kym_s2d_filter_shape(h, 0, ctypes.byref(r), ctypes.byref(c)) == 0 and (r.value, c.value) == (Mp, Np)
+    assert lib.kym_s2d_filter_shape(h, nf, ctypes.byref(r), ctypes.byref(c)) != 0
+    assert lib.kym_s2d_workspace_bytes(h, 4) > 0
+    assert lib.kym_s2d_plan_destroy(h) == 0
+
+
+def test_plan_rejects_bad_geometry(lib):
+    from kymatio_gb300 import _lib
+    h = _lib._vp()
+    assert lib.kym_s2d_plan_create(10, 10, 10, 8, 2, 0, ctypes.byref(h)) == _lib.KYM_ERR_INVALID
+    assert lib.kym_s2d_plan_create(0, 10, 1, 8, 2, 0, ctypes.byref(h)) == _lib.KYM_ERR_INVALID
+    assert lib.kym_s2d_plan_create(32, 32, 2, 8, 3, 0, ctypes.byref(h)) == _lib.KYM_ERR_INVALID
+    assert lib.kym_s2d_forward(None, None, None, 0, None, 0, None, 0, None) == _lib.KYM_ERR_INVALID
+
+
+def test_product_bank_matches_reference():
+    from kymatio_gb300.filter_bank import filter_bank_2d
+    d = np.load(os.path.join(GOLDEN, 'ref_bank_2d.npz'))
+    phi, psi = filter_bank_2d(40, 40, 2, 8)
+    for r, lv in enumerate(phi):
+        assert np.array_equal(lv, d['phi/%d' % r])
+    for n, p in enumerate(psi):
+        for r, lv in enumerate(p['levels']):
+            assert np.array_equal(lv, d['psi/%d/%d' % (n, r)])
+
+
+def test_product_bank_checksums_272():
+    from kymatio_gb300.filter_bank import filter_bank_2d
+    d = np.load(os.path.join(GOLDEN, 'ref_bank_2d.npz'))['big272/checksums']
+    phi, psi = filter_bank_2d(272, 272, 3, 8)
+    levels = list(phi) + [lv for p in psi for lv in p['levels']]
+    got = np.array([[lv.sum(dtype=np.float64), (lv.astype(np.float64) ** 2).sum(), lv[0, 0], lv[3, 5]]
+                    for lv in levels])
+    assert got.shape == d.shape
+    assert np.array_equal(got, d)
