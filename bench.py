@@ -27,7 +27,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-J, L, SIDE, BATCH = 3, 8, 256, 64
+J, L, SIDE = 3, 8, 256
+BATCH = 64
 METRIC = 'Scattering2D 256^2 J=3 L=8 img/s'
 
 
@@ -354,7 +355,10 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--chunk', type=int, default=0)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--batch', type=int, default=64, help='images per GPU (64 is the benchmark workload)')
     args = ap.parse_args()
+    global BATCH
+    BATCH = args.batch
     args.warmup = max(args.warmup, 3)
     if args.impl == 'reference':
         world, rank = int(os.environ.get('WORLD_SIZE', '1')), int(os.environ.get('RANK', '0'))

@@ -33,6 +33,11 @@ extern "C" {
 const char* kym_version(void);
 /* Message for the last CUDA error this thread saw inside the library. */
 const char* kym_last_error(void);
+/* Plans created after this call use the compile-time specialised kernels for
+ * the sizes that have one (enable=1, the default) or the runtime-planned
+ * kernels everywhere (enable=0, for cross-checks).  Returns the previous
+ * setting. */
+int kym_set_specialized(int enable);
 
 /* ------------------------------------------------------------------------
  * 2-D scattering (replaces the forward of ScatteringTorch2D,
@@ -62,7 +67,8 @@ int kym_s2d_get_chunk(const kym_s2d_plan* plan);
 size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch);
 /* The forward runs as launch groups (input stage, one per order-1 scale, one
  * per order-2 scale pair); these describe them: level 0/1/2, tasks per
- * image, work size, fold factor from the parent spectrum, CTAs per task. */
+ * image, work size, fold factor from the parent spectrum, CTAs per task
+ * (negative when the group runs the runtime-planned kernel). */
 int kym_s2d_group_count(const kym_s2d_plan* plan);
 int kym_s2d_group_info(const kym_s2d_plan* plan, int group, int* level, int* ntasks, int* rows, int* cols, int* fold,
                        int* cluster);

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -13,6 +14,7 @@
 
 #include "../../include/kymatio_gb300.h"
 #include "cascade.cuh"
+#include "ct_cascade.cuh"
 #include "plan_util.h"
 
 namespace kym {
@@ -212,6 +214,8 @@ namespace {
 
 struct Group {
   CascadeLaunch L;       // pointers filled at launch
+  bool has_ct = false;   // a compile-time specialised variant exists
+  CtEntry ct{};
   std::vector<Task> tasks;
   size_t task_off = 0;   // offset into the device task array
   size_t smem = 0;
@@ -220,6 +224,7 @@ struct Group {
 };
 
 int odd_pitch(int n) { return (n % 2 == 0) ? n + 1 : n; }
+std::atomic<bool> g_use_ct{true};
 int swz_len(int n) { return n + (n >> 4) + 1; }
 
 }  // namespace
@@ -341,6 +346,15 @@ static int make_group(CascadePlan* P, Group& g, int mr, int mc, int kr, int kc, 
     L.cluster = C;
     L.rows_local = mr / C;
   }
+  static_assert(sizeof(int) == 4, "");
+  if (g_use_ct) {
+    const CtEntry* e = ct_find(mr, mc, sr, sc, L.cluster, P->oned);
+    if (e && e->smem <= max_smem) {
+      g.has_ct = true;
+      g.ct = *e;
+      g.smem = e->smem;
+    }
+  }
   L.load_scale = src_image ? 1.f : (float)(1.0 / ((double)kr * kc) / (modulus ? (double)mr * mc : 1.0));
   L.s_scale = (float)(1.0 / ((double)(mr / sr) * (mc / sc)) / ((double)sr * sc));
   return KYM_OK;
@@ -451,7 +465,8 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
           cudaEventCreate(&e1);
           cudaEventRecord(e0, stream);
         }
-        if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
+        if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
+        else if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
         else if (Li.cluster > 1) err = launch_group<true, false>(g, Li, F, ni, stream);
         else err = launch_group<false, false>(g, Li, F, ni, stream);
         if (e0) {
@@ -631,6 +646,10 @@ fail:
   return rc;
 }
 
+extern "C" int kym_set_specialized(int enable) {
+  return kym::g_use_ct.exchange(enable != 0) ? 1 : 0;
+}
+
 extern "C" int kym_s2d_plan_destroy(kym_s2d_plan* plan) {
   delete plan;
   return KYM_OK;
@@ -677,7 +696,7 @@ extern "C" int kym_s2d_group_info(const kym_s2d_plan* plan, int group, int* leve
   if (rows) *rows = g.L.mr;
   if (cols) *cols = g.L.mc;
   if (fold) *fold = g.L.kc;
-  if (cluster) *cluster = g.L.cluster;
+  if (cluster) *cluster = g.L.cluster * (g.has_ct ? 1 : -1);
   return KYM_OK;
 }
 

@@ -1,0 +1,242 @@
+// Compile-time specialised variant of the fused cascade kernel (see
+// cascade.cu for the algorithm).  MR x MC is the work size, SR x SC the
+// low-pass output size, C the CTAs per task (rows split over a cluster),
+// ONED a single row with a swizzled layout, NT the CTA size.
+#pragma once
+#include "cascade.cuh"
+#include "ct_engine.cuh"
+
+namespace kym {
+
+using CtLauncher = cudaError_t (*)(const CascadeLaunch&, const FilterTable&, int nimg, cudaStream_t);
+
+struct CtEntry {
+  int mr, mc, sr, sc, c;
+  bool oned;
+  size_t smem;
+  CtLauncher fn;
+};
+
+// Registry of the instantiated variants (filled by static initialisers).
+void ct_register(const CtEntry& e);
+const CtEntry* ct_find(int mr, int mc, int sr, int sc, int c, bool oned);
+
+__device__ __forceinline__ int ct_reflect(int i, int n) {
+  if (n == 1) return 0;
+  const int period = 2 * (n - 1);
+  i %= period;
+  if (i < 0) i += period;
+  return i < n ? i : period - i;
+}
+
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
+struct CtGeom {
+  static constexpr int RL = MR / C;                                  // rows per CTA
+  static constexpr int LD = ONED ? MC + (MC >> 4) + 1 : (MC % 2 == 0 ? MC + 1 : MC);
+  static constexpr int LDB = ONED ? SC + (SC >> 4) + 1 : (SC % 2 == 0 ? SC + 1 : SC);
+  static constexpr size_t smem = ((size_t)RL * LD + (size_t)SR * LDB) * sizeof(float2);
+  static_assert(MR % C == 0 && MC % C == 0, "cluster split");
+  static_assert(MR % SR == 0 && MC % SC == 0, "low-pass fold");
+};
+
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    ct_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
+  using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
+  constexpr int RL = G::RL, LD = G::LD, LDB = G::LDB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* A = reinterpret_cast<float2*>(smem_raw);
+  float2* B = A + RL * LD;
+  int rank = 0;
+  if constexpr (C > 1) rank = static_cast<int>(cg::this_cluster().block_rank());
+  const int task_id = blockIdx.x / C;
+  const int img = blockIdx.y;
+  const Task t = L.tasks[task_id];
+  const int row0 = rank * RL;
+
+  auto at = [&](int u, int v) -> float2* {
+    if constexpr (ONED) return A + (v + (v >> 4));
+    else return A + u * LD + v;
+  };
+
+  // ---- load ------------------------------------------------------------------
+  constexpr int NLOC = RL * MC;
+  if (L.src_image) {
+    const float* x = L.x + (size_t)(L.img0 + img) * L.x_stride;
+    for (int e = threadIdx.x; e < NLOC; e += NT) {
+      const int u = e / MC, v = e % MC;
+      const int iy = ONED ? 0 : ct_reflect(row0 + u - L.pad_t, L.img_M);
+      const int ix = ct_reflect(v - L.pad_l, L.img_N);
+      *at(u, v) = make_float2(__ldg(x + (size_t)iy * L.img_N + ix) * L.load_scale, 0.f);
+    }
+  } else {
+    const float2* src = L.src + (size_t)img * L.src_stride + t.src_off;
+    const float* psi = F.f[t.psi];
+    const int kr = L.kr, kc = L.kc;
+    const int scols = kc * MC;
+    for (int e = threadIdx.x; e < NLOC; e += NT) {
+      const int u = e / MC, v = e % MC;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int a = 0; a < kr; ++a) {
+        const size_t rb = (size_t)(row0 + u + a * MR) * scols + v;
+#pragma unroll 4
+        for (int b = 0; b < kc; ++b) {
+          const size_t idx = rb + (size_t)b * MC;
+          const float2 s = __ldg(src + idx);
+          const float f = __ldg(psi + idx);
+          acc.x = fmaf(s.x, f, acc.x);
+          acc.y = fmaf(s.y, f, acc.y);
+        }
+      }
+      *at(u, v) = cscale(acc, L.load_scale);
+    }
+  }
+  __syncthreads();
+
+  const ct::RowLines<LD, ONED> rows{A};
+  if (L.modulus) {
+    ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, true);
+    if constexpr (!ONED) {
+      if constexpr (C > 1) {
+        ct::cluster_sync();
+        const ct::ClusterColLines<LD, RL> cols{ct::smem_u32(A)};
+        ct::fft_lines<MR, MC / C, NT>(cols, rank * (MC / C), L.pcol.tw, true);
+      } else {
+        const ct::ColLines<LD> cols{A};
+        ct::fft_lines<MR, MC, NT>(cols, 0, L.pcol.tw, true);
+      }
+    }
+    for (int e = threadIdx.x; e < NLOC; e += NT) {
+      float2* p = at(e / MC, e % MC);
+      const float2 z = *p;
+      *p = make_float2(sqrtf(fmaf(z.x, z.x, z.y * z.y)), 0.f);
+    }
+    if constexpr (!ONED) {
+      if constexpr (C > 1) {
+        ct::cluster_sync();
+        const ct::ClusterColLines<LD, RL> cols{ct::smem_u32(A)};
+        ct::fft_lines<MR, MC / C, NT>(cols, rank * (MC / C), L.pcol.tw, false);
+      } else {
+        __syncthreads();
+        const ct::ColLines<LD> cols{A};
+        ct::fft_lines<MR, MC, NT>(cols, 0, L.pcol.tw, false);
+      }
+    } else {
+      __syncthreads();
+    }
+    ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, false);
+  } else {
+    ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, false);
+    if constexpr (!ONED) {
+      if constexpr (C > 1) {
+        ct::cluster_sync();
+        const ct::ClusterColLines<LD, RL> cols{ct::smem_u32(A)};
+        ct::fft_lines<MR, MC / C, NT>(cols, rank * (MC / C), L.pcol.tw, false);
+      } else {
+        const ct::ColLines<LD> cols{A};
+        ct::fft_lines<MR, MC, NT>(cols, 0, L.pcol.tw, false);
+      }
+    }
+  }
+
+  // ---- parent spectrum for the next order --------------------------------------
+  if (t.dst_off >= 0) {
+    float2* dst = L.dst + (size_t)img * L.dst_stride + t.dst_off + (size_t)row0 * MC;
+    for (int e = threadIdx.x; e < NLOC; e += NT) dst[e] = *at(e / MC, e % MC);
+  }
+
+  // ---- low-pass: partial fold over local rows --------------------------------------
+  constexpr int KSR = MR / SR, KSC = MC / SC;
+  const float* phi = F.f[t.phi];
+  for (int e = threadIdx.x; e < SR * SC; e += NT) {
+    const int p = e / SC, q = e % SC;
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < KSR; ++a) {
+      const int g = p + a * SR;
+      if (C > 1 && (g < row0 || g >= row0 + RL)) continue;
+#pragma unroll
+      for (int b = 0; b < KSC; ++b) {
+        const int col = q + b * SC;
+        const float2 z = *at(g - row0, col);
+        const float f = __ldg(phi + (size_t)g * MC + col);
+        acc.x = fmaf(z.x, f, acc.x);
+        acc.y = fmaf(z.y, f, acc.y);
+      }
+    }
+    float2* bp = ONED ? B + (q + (q >> 4)) : B + p * LDB + q;
+    *bp = cscale(acc, L.s_scale);
+  }
+  if constexpr (C > 1) {
+    ct::cluster_sync();
+    if (rank == 0) {
+      for (int e = threadIdx.x; e < SR * SC; e += NT) {
+        float2* bp = B + (e / SC) * LDB + (e % SC);
+        float2 acc = *bp;
+        const uint32_t a = ct::smem_u32(bp);
+#pragma unroll
+        for (int r = 1; r < C; ++r) acc = cadd(acc, ct::ld_dsmem(ct::mapa(a, r)));
+        *bp = acc;
+      }
+    }
+    ct::cluster_sync();
+    if (rank != 0) return;
+  }
+  __syncthreads();
+
+  // ---- small inverse transform, real part, unpad ------------------------------------
+  const ct::RowLines<LDB, ONED> brows{B};
+  ct::fft_lines<SC, SR, NT>(brows, 0, L.psrow.tw, true);
+  if constexpr (!ONED) {
+    const ct::ColLines<LDB> bcols{B};
+    ct::fft_lines<SR, SC, NT>(bcols, 0, L.pscol.tw, true);
+  }
+  float* out = L.out + (size_t)(L.img0 + img) * L.out_stride + (size_t)t.out_ch * L.out_nr * L.out_nc;
+  for (int e = threadIdx.x; e < L.out_nr * L.out_nc; e += NT) {
+    const int p = e / L.out_nc + L.out_r0, q = e % L.out_nc + L.out_c0;
+    const float2* bp = ONED ? B + (q + (q >> 4)) : B + p * LDB + q;
+    out[e] = bp->x;
+  }
+}
+
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
+cudaError_t ct_launch(const CascadeLaunch& L, const FilterTable& F, int nimg, cudaStream_t stream) {
+  using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
+  auto kern = ct_cascade_kernel<MR, MC, SR, SC, C, ONED, NT>;
+  static bool configured = false;  // per process; attributes are per function
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(L.ntasks * C, nimg, 1);
+  cfg.blockDim = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes = G::smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  cfg.attrs = attr;
+  cfg.numAttrs = 0;
+  if (C > 1) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, kern, L, F);
+}
+
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
+struct CtRegistrar {
+  CtRegistrar() {
+    using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
+    ct_register(CtEntry{MR, MC, SR, SC, C, ONED, G::smem, &ct_launch<MR, MC, SR, SC, C, ONED, NT>});
+  }
+};
+
+#define KYM_CT_VARIANT(MR, MC, SR, SC, C, ONED, NT) \
+  static ::kym::CtRegistrar<MR, MC, SR, SC, C, ONED, NT> kym_ct_reg_##MR##_##MC##_##SR##_##SC##_##C##_##ONED;
+
+}  // namespace kym

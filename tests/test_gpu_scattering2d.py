@@ -183,3 +183,26 @@ def test_input_size_agnostic():
         x = torch.zeros((3, 3) + shape, device=dev)
         S = Scattering2D(5, shape).to(dev)(x)
         assert S.shape[-2:] == (1, 1)
+
+
+@pytest.mark.parametrize('J,side', [(2, 32), (3, 64), (3, 256), (4, 128)])
+def test_specialised_and_runtime_kernels_agree(J, side):
+    """The compile-time specialised variants and the runtime-planned kernel
+    compute the same transform (both checked against the FP64 oracle)."""
+    dev = _cuda()
+    from kymatio_gb300 import Scattering2D, _lib
+    from oracle.scattering2d import Scattering2D as Oracle
+    lib = _lib.load()
+    x = np.random.default_rng(5).random((2, side, side)).astype(np.float32)
+    ref = Oracle(J, (side, side))(x.astype(np.float64))
+    outs = []
+    for spec in (1, 0):
+        prev = lib.kym_set_specialized(spec)
+        try:
+            sc = Scattering2D(J, (side, side)).to(dev)
+            outs.append(sc(torch.from_numpy(x).to(dev)).cpu().numpy())
+        finally:
+            lib.kym_set_specialized(prev)
+    for o in outs:
+        _check_orders(o, ref, J, 8, 2)
+    assert rel_l2(outs[0], outs[1]) < 2e-6
