@@ -77,6 +77,11 @@ def build(force=False, verbose=False, jobs=None):
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda s: _compile(s, force, verbose), srcs))
+    keep = set(objs)
+    for f in os.listdir(BUILD_DIR):  # drop objects of older source versions
+        p = os.path.join(BUILD_DIR, f)
+        if f.endswith('.o') and p not in keep:
+            os.remove(p)
     stamp = hashlib.sha1(''.join(objs).encode()).hexdigest()[:16]
     stamp_file = LIB + '.stamp'
     if (not force and os.path.exists(LIB) and os.path.exists(stamp_file)

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -16,6 +17,7 @@
 #include "cascade.cuh"
 #include "ct_cascade.cuh"
 #include "plan_util.h"
+#include "errors.h"
 
 namespace kym {
 
@@ -392,38 +394,57 @@ static cudaError_t launch_group(const Group& g, const CascadeLaunch& L, const Fi
   return cudaLaunchKernelEx(&cfg, kern, L, F);
 }
 
-static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
-                    int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
-                    float* group_ms = nullptr, int max_groups = 0) {
-  if (!P || !x || !out || batch < 0) return KYM_ERR_INVALID;
-  if (batch == 0) return KYM_OK;
-  if (nfilters != (int)P->filter_rows.size() || nfilters > kMaxFilters) return KYM_ERR_INVALID;
-  FilterTable F;
-  std::memset(&F, 0, sizeof(F));
-  for (int i = 0; i < nfilters; ++i) {
-    if (!filters[i]) return KYM_ERR_INVALID;
-    F.f[i] = filters[i];
+// Where one forward finds its tables and workspace.  ``stage0_per_chunk``
+// runs the input stage chunk by chunk (the workspace then holds the input
+// spectra of one chunk only).
+struct RunArgs {
+  const DeviceState* ds = nullptr;
+  float2* u0 = nullptr;
+  float2* u1 = nullptr;
+  int chunk = 1;
+  bool stage0_per_chunk = false;
+  float* group_ms = nullptr;
+  int max_groups = 0;
+};
+
+static int fail_cuda(cudaError_t e, const char* what) {
+  set_error_message(what, cudaGetErrorString(e));
+  return KYM_ERR_CUDA;
+}
+
+static int make_filter_table(CascadePlan* P, const float* const* filters, int nfilters, FilterTable* F) {
+  if (!filters || nfilters != (int)P->filter_rows.size() || nfilters > kMaxFilters) {
+    set_error_message("filters", "filter count does not match the plan");
+    return KYM_ERR_INVALID;
   }
-  const int chunk = std::min(batch, P->chunk);
-  const size_t need = ((size_t)batch * P->u0_elems + (size_t)chunk * P->u1_elems) * sizeof(float2);
-  if (!workspace || ws_bytes < need) return KYM_ERR_WORKSPACE;
-  const DeviceState* ds = device_state(P);
-  if (!ds) return KYM_ERR_CUDA;
-  float2* u0 = static_cast<float2*>(workspace);
-  float2* u1 = u0 + (size_t)batch * P->u0_elems;
+  std::memset(F, 0, sizeof(*F));
+  for (int i = 0; i < nfilters; ++i) {
+    if (!filters[i]) {
+      set_error_message("filters", "null filter pointer");
+      return KYM_ERR_INVALID;
+    }
+    F->f[i] = filters[i];
+  }
+  return KYM_OK;
+}
+
+static int run_core(CascadePlan* P, const float* x, float* out, int batch, const FilterTable& F, const RunArgs& a,
+                    cudaStream_t stream) {
+  const DeviceState* ds = a.ds;
+  const int chunk = std::max(1, std::min(batch, a.chunk));
   const long long x_stride = (long long)P->img_M * P->img_N;
   const long long out_stride = (long long)P->channels * P->out_nr * P->out_nc;
   cudaError_t err = cudaSuccess;
   // optional timing: one event pair around every launch of every group
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> evs;
-  const bool timed = group_ms && max_groups > 0;
+  const bool timed = a.group_ms && a.max_groups > 0;
   if (timed)
-    for (int i = 0; i < max_groups; ++i) group_ms[i] = 0.f;
+    for (int i = 0; i < a.max_groups; ++i) a.group_ms[i] = 0.f;
   for (int c0 = 0; c0 < batch; c0 += chunk) {
     const int nimg = std::min(chunk, batch - c0);
     for (size_t gi = 0; gi < P->groups.size(); ++gi) {
       const Group& g = P->groups[gi];
-      if (g.level == 0 && c0 != 0) continue;  // the input stage runs once over the batch
+      if (g.level == 0 && c0 != 0 && !a.stage0_per_chunk) continue;  // input stage once over the batch
       CascadeLaunch L = g.L;
       L.tasks = ds->tasks + g.task_off;
       L.ntasks = (int)g.tasks.size();
@@ -436,20 +457,23 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
       L.out = out;
       L.out_stride = out_stride;
       int n = nimg;
+      // image c of the chunk has its input spectrum at u0 + i * u0_elems, with
+      // i = c0 + c when the input stage covers the whole batch, i = c otherwise
+      const size_t u0_first = a.stage0_per_chunk ? 0 : (size_t)c0;
       if (g.level == 0) {
-        n = batch;
-        L.img0 = 0;
-        L.dst = u0;
+        n = a.stage0_per_chunk ? nimg : batch;
+        L.img0 = a.stage0_per_chunk ? c0 : 0;
+        L.dst = a.u0;
         L.dst_stride = P->u0_elems;
       } else if (g.level == 1) {
         L.img0 = c0;
-        L.src = u0 + (size_t)c0 * P->u0_elems;
+        L.src = a.u0 + u0_first * P->u0_elems;
         L.src_stride = P->u0_elems;
-        L.dst = u1;
+        L.dst = a.u1;
         L.dst_stride = P->u1_elems;
       } else {
         L.img0 = c0;
-        L.src = u1;
+        L.src = a.u1;
         L.src_stride = P->u1_elems;
       }
       // grid.y is limited to 65535 images per launch
@@ -460,7 +484,7 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
         if (Li.src) Li.src = L.src + (size_t)i0 * L.src_stride;
         if (Li.dst) Li.dst = L.dst + (size_t)i0 * L.dst_stride;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
-        if (timed && (int)gi < max_groups) {
+        if (timed && (int)gi < a.max_groups) {
           cudaEventCreate(&e0);
           cudaEventCreate(&e1);
           cudaEventRecord(e0, stream);
@@ -478,22 +502,101 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
             cudaEventDestroy(e.second.first);
             cudaEventDestroy(e.second.second);
           }
-          return KYM_ERR_CUDA;
+          return fail_cuda(err, "cascade launch");
         }
       }
     }
   }
   if (timed) {
-    if (cudaStreamSynchronize(stream) != cudaSuccess) err = cudaErrorUnknown;
+    cudaError_t se = cudaStreamSynchronize(stream);
     for (auto& e : evs) {
       float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, e.second.first, e.second.second) == cudaSuccess) group_ms[e.first] += ms;
+      if (cudaEventElapsedTime(&ms, e.second.first, e.second.second) == cudaSuccess) a.group_ms[e.first] += ms;
       cudaEventDestroy(e.second.first);
       cudaEventDestroy(e.second.second);
     }
-    if (err != cudaSuccess) return KYM_ERR_CUDA;
+    if (se != cudaSuccess) return fail_cuda(se, "timed forward");
   }
   return KYM_OK;
+}
+
+static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
+                    int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
+                    float* group_ms = nullptr, int max_groups = 0) {
+  if (!P || !x || !out || batch < 0) {
+    set_error_message("forward", "null plan, input or output");
+    return KYM_ERR_INVALID;
+  }
+  if (batch == 0) return KYM_OK;
+  FilterTable F;
+  int rc = make_filter_table(P, filters, nfilters, &F);
+  if (rc) return rc;
+  const int chunk = std::min(batch, P->chunk);
+  const size_t need = ((size_t)batch * P->u0_elems + (size_t)chunk * P->u1_elems) * sizeof(float2);
+  if (!workspace || ws_bytes < need) {
+    set_error_message("forward", "workspace missing or smaller than the plan requires");
+    return KYM_ERR_WORKSPACE;
+  }
+  const DeviceState* ds = device_state(P);
+  if (!ds) return fail_cuda(cudaGetLastError(), "plan table upload");
+  RunArgs a;
+  a.ds = ds;
+  a.u0 = static_cast<float2*>(workspace);
+  a.u1 = a.u0 + (size_t)batch * P->u0_elems;
+  a.chunk = chunk;
+  a.group_ms = group_ms;
+  a.max_groups = max_groups;
+  return run_core(P, x, out, batch, F, a, stream);
+}
+
+// Forward whose tables and workspace live in a caller-provided device buffer
+// (the library's static scratch): the plan's task and twiddle tables are
+// copied to its head on `stream`, then the batch runs in chunks whose input
+// and parent spectra fit the rest.
+int run_plan_in_scratch(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
+                        int nfilters, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  if (!P || !x || !out || batch < 0 || !scratch) {
+    set_error_message("forward_noalloc", "null plan, input, output or scratch");
+    return KYM_ERR_INVALID;
+  }
+  if (batch == 0) return KYM_OK;
+  FilterTable F;
+  int rc = make_filter_table(P, filters, nfilters, &F);
+  if (rc) return rc;
+  const size_t nt = P->all_tasks.size(), nw = P->tw.host().size();
+  const size_t tasks_bytes = (nt * sizeof(Task) + 255) & ~size_t(255);
+  const size_t tw_bytes = (nw * sizeof(float2) + 255) & ~size_t(255);
+  const size_t tables = tasks_bytes + tw_bytes;
+  const size_t per_image = (size_t)(P->u0_elems + P->u1_elems) * sizeof(float2);
+  if (tables + per_image > scratch_bytes) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "one image needs %zu bytes of scratch (tables %zu + spectra %zu), above the %zu-byte static "
+                  "scratch of the allocation-free entry point",
+                  tables + per_image, tables, per_image, scratch_bytes);
+    set_error_message("forward_noalloc", msg);
+    return KYM_ERR_WORKSPACE;
+  }
+  unsigned char* base = static_cast<unsigned char*>(scratch);
+  // tables: copied on the stream, so earlier calls on the same stream finish first
+  std::vector<unsigned char> img(tables, 0);
+  if (nt) std::memcpy(img.data(), P->all_tasks.data(), nt * sizeof(Task));
+  if (nw) std::memcpy(img.data() + tasks_bytes, P->tw.host().data(), nw * sizeof(float2));
+  cudaError_t e = cudaMemcpyAsync(base, img.data(), tables, cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return fail_cuda(e, "scratch table copy");
+  DeviceState ds;
+  ds.tasks = reinterpret_cast<Task*>(base);
+  ds.tw = reinterpret_cast<float2*>(base + tasks_bytes);
+  const int fit = (int)std::min<size_t>((scratch_bytes - tables) / per_image, (size_t)1 << 20);
+  RunArgs a;
+  a.ds = &ds;
+  a.chunk = std::max(1, std::min(fit, P->chunk));
+  a.u0 = reinterpret_cast<float2*>(base + tables);
+  a.u1 = a.u0 + (size_t)a.chunk * P->u0_elems;
+  a.stage0_per_chunk = true;
+  // a copy from pageable memory returns once the host image is staged, so
+  // `img` may go out of scope before the transfer completes
+  return run_core(P, x, out, batch, F, a, stream);
 }
 
 static void set_default_chunk(CascadePlan* P) {
@@ -714,6 +817,10 @@ extern "C" size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch) {
   const int chunk = std::min(batch, P.chunk);
   return ((size_t)batch * P.u0_elems + (size_t)chunk * P.u1_elems) * sizeof(float2);
 }
+
+namespace kym {
+CascadePlan* plan_of(const kym_s2d_plan* p) { return const_cast<CascadePlan*>(&p->p); }
+}  // namespace kym
 
 extern "C" int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch,
                                const float* const* filters, int n_filters, void* workspace,
