@@ -83,6 +83,25 @@ int kym_s2d_forward_timed(const kym_s2d_plan* plan, const float* x, float* out, 
 int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
                     int n_filters, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Allocation-free forward.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory (a fixed memory pool reserved up
+ * front, a host application that forbids allocation after start-up).  It
+ * computes exactly what kym_s2d_forward computes, but needs no workspace
+ * argument: the plan's tables and the spectra of one chunk of images live in
+ * a static device array of KYM_NOALLOC_SCRATCH_BYTES inside the library,
+ * which every GPU that loads the library holds until the process exits.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine.
+ *   - The first call on a device looks the array's address up
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call shares the one array: calls that overlap on the GPU (on
+ *     different streams, or from different threads) race and corrupt each
+ *     other's results; serialise them on one stream.
+ *   - Returns KYM_ERR_WORKSPACE when one image's spectra plus the plan's tables
+ *     exceed the array (kym_last_error() gives the sizes). */
+#define KYM_NOALLOC_SCRATCH_BYTES (32u << 20)
+int kym_s2d_forward_noalloc(const kym_s2d_plan* plan, const float* x, float* out, int batch,
+                            const float* const* filters, int n_filters, void* stream);
+
 /* ------------------------------------------------------------------------
  * 1-D scattering, local averaging (replaces ScatteringBase1D.scattering with
  * average='local', kymatio/scattering1d/frontend/base_frontend.py:106-155,
