@@ -83,6 +83,20 @@ int kym_s2d_forward_timed(const kym_s2d_plan* plan, const float* x, float* out, 
 int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
                     int n_filters, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Hand-written backward: grad_x (batch, M, N) = (d forward / d x)^T grad_out,
+ * grad_out shaped like the forward's output.  Replaces torch autograd through
+ * the reference op surface (unpad, irfft, subsample_fourier, cdgmm, rfft,
+ * ModulusStable.backward of kymatio/backend/torch_backend.py:85-96, ifft,
+ * ReflectionPad2d).  Recomputes the input and parent spectra chunk by chunk
+ * into the workspace (kym_s2d_backward_workspace_bytes). */
+size_t kym_s2d_backward_workspace_bytes(const kym_s2d_plan* plan, int batch);
+/* Images per backward pass (bounds its workspace: the recomputed input and
+ * parent spectra and the per-path gradient blocks of one chunk). */
+int kym_s2d_set_backward_chunk(kym_s2d_plan* plan, int chunk);
+int kym_s2d_backward(const kym_s2d_plan* plan, const float* x, const float* grad_out, float* grad_x, int batch,
+                     const float* const* filters, int n_filters, void* workspace, size_t workspace_bytes,
+                     void* stream);
+
 /* Allocation-free forward.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (a fixed memory pool reserved up
  * front, a host application that forbids allocation after start-up).  It
@@ -126,6 +140,12 @@ size_t kym_s1d_workspace_bytes(const kym_s1d_plan* plan, int batch);
  * kymatio/scattering1d/frontend/torch_frontend.py:30-56). */
 int kym_s1d_forward(const kym_s1d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
                     int n_filters, void* workspace, size_t workspace_bytes, void* stream);
+/* Backward of kym_s1d_forward (ModulusStable.backward and the adjoints of the
+ * 1-D op surface, kymatio/scattering1d/backend/torch_backend.py:18-141). */
+size_t kym_s1d_backward_workspace_bytes(const kym_s1d_plan* plan, int batch);
+int kym_s1d_backward(const kym_s1d_plan* plan, const float* x, const float* grad_out, float* grad_x, int batch,
+                     const float* const* filters, int n_filters, void* workspace, size_t workspace_bytes,
+                     void* stream);
 
 #ifdef __cplusplus
 }

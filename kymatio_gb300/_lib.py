@@ -36,6 +36,9 @@ SIGNATURES = {
     'kym_s2d_workspace_bytes': (_c_size, [_vp, _c_int]),
     'kym_s2d_forward': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
     'kym_s2d_forward_noalloc': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp]),
+    'kym_s2d_backward_workspace_bytes': (_c_size, [_vp, _c_int]),
+    'kym_s2d_set_backward_chunk': (_c_int, [_vp, _c_int]),
+    'kym_s2d_backward': (_c_int, [_vp, _vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
     'kym_s2d_group_count': (_c_int, [_vp]),
     'kym_s2d_group_info': (_c_int, [_vp, _c_int] + [_ip] * 6),
     'kym_s2d_forward_timed': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp,
@@ -47,6 +50,8 @@ SIGNATURES = {
     'kym_s1d_set_chunk': (_c_int, [_vp, _c_int]),
     'kym_s1d_workspace_bytes': (_c_size, [_vp, _c_int]),
     'kym_s1d_forward': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
+    'kym_s1d_backward_workspace_bytes': (_c_size, [_vp, _c_int]),
+    'kym_s1d_backward': (_c_int, [_vp, _vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
 }
 
 _lock = threading.Lock()

@@ -16,6 +16,7 @@
 #include "../../include/kymatio_gb300.h"
 #include "cascade.cuh"
 #include "ct_cascade.cuh"
+#include "bwd.cuh"
 #include "plan_util.h"
 #include "errors.h"
 
@@ -148,6 +149,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   }
 
+  if (L.skip_s) return;  // no remote shared-memory access follows the last cluster barrier
+
   // ---- low-pass branch: B = fold(A * phi) (partial over local rows) --------
   const float* phi = F.f[t.phi];
   const int sr = L.sr, sc = L.sc;
@@ -234,6 +237,19 @@ int swz_len(int n) { return n + (n >> 4) + 1; }
 struct DeviceState {
   Task* tasks = nullptr;
   float2* tw = nullptr;
+  BwdTask* btasks = nullptr;
+  GatherItem* gather = nullptr;
+};
+
+// Backward launch group: mirrors one forward group's geometry.
+struct BwdGroup {
+  int fwd = 0;                 // index of the forward group it mirrors
+  int level = 0;
+  std::vector<BwdTask> tasks;
+  size_t task_off = 0;
+  bool has_ct = false;
+  size_t smem = 0;             // shared memory of the launched variant
+  BwdCtLauncher ct = nullptr;
 };
 
 struct CascadePlan {
@@ -249,6 +265,12 @@ struct CascadePlan {
   int chunk = 0;
   std::vector<Group> groups;
   std::vector<Task> all_tasks;
+  // backward
+  std::vector<BwdGroup> bgroups;
+  std::vector<BwdTask> all_btasks;
+  std::vector<GatherItem> all_gather;
+  long long gy1_elems = 0, gy2_elems = 0;  // per image: order-1 / order-2 gradient blocks (complex)
+  int bchunk = 0;
   TwiddleBank tw;
   std::mutex mu;                     // guards `dev`
   std::map<int, DeviceState> dev;    // task and twiddle tables, per device
@@ -259,6 +281,8 @@ struct CascadePlan {
       if (cudaSetDevice(kv.first) != cudaSuccess) continue;
       cudaFree(kv.second.tasks);
       cudaFree(kv.second.tw);
+      cudaFree(kv.second.btasks);
+      cudaFree(kv.second.gather);
     }
     if (have) cudaSetDevice(cur);
     cudaGetLastError();
@@ -291,10 +315,18 @@ static const DeviceState* device_state(CascadePlan* P) {
     cudaFree(s.tasks);
     return nullptr;
   }
-  if ((nt && cudaMemcpy(s.tasks, P->all_tasks.data(), nt * sizeof(Task), cudaMemcpyHostToDevice) != cudaSuccess) ||
-      (nw && cudaMemcpy(s.tw, P->tw.host().data(), nw * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)) {
+  const size_t nb = P->all_btasks.size(), ng = P->all_gather.size();
+  if (cudaMalloc(&s.btasks, std::max<size_t>(nb, 1) * sizeof(BwdTask)) != cudaSuccess ||
+      cudaMalloc(&s.gather, std::max<size_t>(ng, 1) * sizeof(GatherItem)) != cudaSuccess ||
+      (nt && cudaMemcpy(s.tasks, P->all_tasks.data(), nt * sizeof(Task), cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (nw && cudaMemcpy(s.tw, P->tw.host().data(), nw * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (nb && cudaMemcpy(s.btasks, P->all_btasks.data(), nb * sizeof(BwdTask), cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (ng && cudaMemcpy(s.gather, P->all_gather.data(), ng * sizeof(GatherItem), cudaMemcpyHostToDevice) !=
+                 cudaSuccess)) {
     cudaFree(s.tasks);
     cudaFree(s.tw);
+    cudaFree(s.btasks);
+    cudaFree(s.gather);
     return nullptr;
   }
   return &(P->dev[d] = s);
@@ -599,6 +631,288 @@ int run_plan_in_scratch(CascadePlan* P, const float* x, float* out, int batch, c
   return run_core(P, x, out, batch, F, a, stream);
 }
 
+// ---------------------------------------------------------------------------
+// backward: tables
+// ---------------------------------------------------------------------------
+static size_t rt_bwd_smem(const CascadeLaunch& L) {
+  return ((size_t)L.rows_local * L.ld + (size_t)L.sr * L.ldb) * sizeof(float2) +
+         (L.cluster > 1 ? (size_t)L.mr * sizeof(void*) : 0);
+}
+
+// Mirror every forward group with a backward group.  Order-2 tasks write
+// g_Y into the per-image order-2 block; order-1 tasks gather their children
+// (the order-2 tasks reading their spectrum) and write into the order-1
+// block; the input stage gathers every order-1 task.
+static int build_backward(CascadePlan* P) {
+  P->bgroups.clear();
+  P->all_btasks.clear();
+  P->all_gather.clear();
+  std::map<long long, std::vector<int>> children;  // parent spectrum offset -> (group<<20 | task)
+  std::vector<std::vector<long long>> gy_of(P->groups.size());
+  long long gy2 = 0, gy1 = 0;
+  for (size_t gi = 0; gi < P->groups.size(); ++gi) {
+    const Group& g = P->groups[gi];
+    gy_of[gi].assign(g.tasks.size(), -1);
+    if (g.level != 2) continue;
+    for (size_t ti = 0; ti < g.tasks.size(); ++ti) {
+      gy_of[gi][ti] = gy2;
+      gy2 += (long long)g.L.mr * g.L.mc;
+      children[g.tasks[ti].src_off].push_back((int)((gi << 20) | ti));
+    }
+  }
+  for (size_t gi = 0; gi < P->groups.size(); ++gi) {
+    const Group& g = P->groups[gi];
+    if (g.level != 1) continue;
+    for (size_t ti = 0; ti < g.tasks.size(); ++ti) {
+      gy_of[gi][ti] = gy1;
+      gy1 += (long long)g.L.mr * g.L.mc;
+    }
+  }
+  P->gy1_elems = gy1;
+  P->gy2_elems = gy2;
+  auto item_of = [&](int gi, int ti) {
+    const Group& c = P->groups[gi];
+    GatherItem it;
+    it.gy_off = gy_of[gi][ti];
+    it.psi = c.tasks[ti].psi;
+    it.mr = c.L.mr;
+    it.mc = c.L.mc;
+    it.kr = c.L.kr;
+    it.kc = c.L.kc;
+    it.pad_ = 0;
+    return it;
+  };
+  for (int level : {2, 1, 0}) {
+    for (size_t gi = 0; gi < P->groups.size(); ++gi) {
+      const Group& g = P->groups[gi];
+      if (g.level != level) continue;
+      BwdGroup b;
+      b.fwd = (int)gi;
+      b.level = level;
+      for (size_t ti = 0; ti < g.tasks.size(); ++ti) {
+        const Task& t = g.tasks[ti];
+        BwdTask bt;
+        bt.src_off = t.src_off;
+        bt.gy_off = level == 0 ? 0 : gy_of[gi][ti];
+        bt.psi = level == 0 ? -1 : t.psi;
+        bt.phi = t.phi;
+        bt.out_ch = t.out_ch;
+        bt.gather_first = (int)P->all_gather.size();
+        bt.gather_count = 0;
+        bt.pad_ = 0;
+        if (level == 1 && t.dst_off >= 0) {
+          auto it = children.find(t.dst_off);
+          if (it != children.end())
+            for (int code : it->second) P->all_gather.push_back(item_of(code >> 20, code & 0xFFFFF));
+        } else if (level == 0) {
+          for (size_t gj = 0; gj < P->groups.size(); ++gj)
+            if (P->groups[gj].level == 1)
+              for (size_t tj = 0; tj < P->groups[gj].tasks.size(); ++tj)
+                P->all_gather.push_back(item_of((int)gj, (int)tj));
+        }
+        bt.gather_count = (int)P->all_gather.size() - bt.gather_first;
+        b.tasks.push_back(bt);
+      }
+      size_t smem = 0;
+      BwdCtLauncher fn = nullptr;
+      if (g.has_ct && bwd_ct_find(g.L.mr, g.L.mc, g.L.sr, g.L.sc, g.L.cluster, g.oned, &smem, &fn)) {
+        b.has_ct = true;
+        b.ct = fn;
+        b.smem = smem;
+      } else {
+        b.smem = rt_bwd_smem(g.L);
+      }
+      b.task_off = P->all_btasks.size();
+      P->all_btasks.insert(P->all_btasks.end(), b.tasks.begin(), b.tasks.end());
+      P->bgroups.push_back(b);
+    }
+  }
+  const double budget = 256.0 * 1024 * 1024;
+  const double per = (double)(P->u0_elems + P->u1_elems + P->gy1_elems + P->gy2_elems) * sizeof(float2);
+  P->bchunk = (int)std::max(1.0, std::min(budget / per, (double)(1 << 20)));
+  return KYM_OK;
+}
+
+static size_t backward_bytes(const CascadePlan* P, int batch) {
+  const int chunk = std::min(batch, P->bchunk);
+  return (size_t)chunk * (P->u0_elems + P->u1_elems + P->gy1_elems + P->gy2_elems) * sizeof(float2);
+}
+
+template <bool CL, bool ONED>
+static cudaError_t launch_rt_bwd(const BwdGroup& b, const BwdLaunch& L, const FilterTable& F, int nimg,
+                                 cudaStream_t stream) {
+  auto kern = rt_bwd_kernel<CL, ONED>;
+  static int configured_device = -1;
+  int d = 0;
+  cudaGetDevice(&d);
+  if (configured_device != d) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)max_dynamic_smem());
+    if (e != cudaSuccess) return e;
+    configured_device = d;
+  }
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(L.ntasks * L.cluster, nimg, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = b.smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  cfg.attrs = attr;
+  cfg.numAttrs = 0;
+  if (CL) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = L.cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, kern, L, F);
+}
+
+// g_x for a batch: per chunk, recompute the input and parent spectra, then
+// run the order-2, order-1 and input-stage backward groups and the
+// reflect-pad adjoint.
+static int run_backward(CascadePlan* P, const float* x, const float* gout, float* gx, int batch,
+                        const float* const* filters, int nfilters, void* workspace, size_t ws_bytes,
+                        cudaStream_t stream) {
+  if (!P || !x || !gout || !gx || batch < 0) {
+    set_error_message("backward", "null plan, input, gradient or output");
+    return KYM_ERR_INVALID;
+  }
+  if (batch == 0) return KYM_OK;
+  FilterTable F;
+  int rc = make_filter_table(P, filters, nfilters, &F);
+  if (rc) return rc;
+  if (!workspace || ws_bytes < backward_bytes(P, batch)) {
+    set_error_message("backward", "workspace missing or smaller than the plan requires");
+    return KYM_ERR_WORKSPACE;
+  }
+  const DeviceState* ds = device_state(P);
+  if (!ds) return fail_cuda(cudaGetLastError(), "plan table upload");
+  const int chunk = std::min(batch, P->bchunk);
+  float2* u0 = static_cast<float2*>(workspace);
+  float2* u1 = u0 + (size_t)chunk * P->u0_elems;
+  float2* gy2 = u1 + (size_t)chunk * P->u1_elems;
+  float2* gy1 = gy2 + (size_t)chunk * P->gy2_elems;
+  const long long gs_stride = (long long)P->channels * P->out_nr * P->out_nc;
+  cudaError_t err = cudaSuccess;
+  for (int c0 = 0; c0 < batch; c0 += chunk) {
+    const int nimg = std::min(chunk, batch - c0);
+    // 1. recompute the spectra the backward needs (input stage, parents)
+    RunArgs a;
+    a.ds = ds;
+    a.u0 = u0;
+    a.u1 = u1;
+    a.chunk = nimg;
+    a.stage0_per_chunk = true;
+    for (size_t gi = 0; gi < P->groups.size(); ++gi) {
+      const Group& g = P->groups[gi];
+      bool needed = g.level == 0;
+      if (g.level == 1)
+        for (const Task& t : g.tasks) needed |= t.dst_off >= 0;
+      if (!needed) continue;
+      CascadeLaunch L = g.L;
+      L.tasks = ds->tasks + g.task_off;
+      L.ntasks = (int)g.tasks.size();
+      L.prow.tw = ds->tw + P->tw.offset(L.prow.n);
+      L.pcol.tw = ds->tw + P->tw.offset(L.pcol.n);
+      L.psrow.tw = ds->tw + P->tw.offset(L.psrow.n);
+      L.pscol.tw = ds->tw + P->tw.offset(L.pscol.n);
+      L.x = x;
+      L.x_stride = (long long)P->img_M * P->img_N;
+      L.img0 = c0;
+      L.skip_s = 1;
+      if (g.level == 0) {
+        L.dst = u0;
+        L.dst_stride = P->u0_elems;
+      } else {
+        L.src = u0;
+        L.src_stride = P->u0_elems;
+        L.dst = u1;
+        L.dst_stride = P->u1_elems;
+      }
+      if (g.has_ct) err = g.ct.fn(L, F, nimg, stream);
+      else if (g.oned) err = launch_group<false, true>(g, L, F, nimg, stream);
+      else if (L.cluster > 1) err = launch_group<true, false>(g, L, F, nimg, stream);
+      else err = launch_group<false, false>(g, L, F, nimg, stream);
+      if (err != cudaSuccess) return fail_cuda(err, "backward recomputation");
+    }
+    // 2. backward groups, order 2 then 1 then the input stage
+    for (const BwdGroup& b : P->bgroups) {
+      const Group& g = P->groups[b.fwd];
+      BwdLaunch L;
+      std::memset(&L, 0, sizeof(L));
+      L.mr = g.L.mr;
+      L.mc = g.L.mc;
+      L.kr = g.L.kr;
+      L.kc = g.L.kc;
+      L.ld = g.L.ld;
+      L.sr = g.L.sr;
+      L.sc = g.L.sc;
+      L.ldb = g.L.ldb;
+      L.cluster = g.L.cluster;
+      L.rows_local = g.L.rows_local;
+      L.prow = g.L.prow;
+      L.pcol = g.L.pcol;
+      L.psrow = g.L.psrow;
+      L.pscol = g.L.pscol;
+      L.prow.tw = ds->tw + P->tw.offset(L.prow.n);
+      L.pcol.tw = ds->tw + P->tw.offset(L.pcol.n);
+      L.psrow.tw = ds->tw + P->tw.offset(L.psrow.n);
+      L.pscol.tw = ds->tw + P->tw.offset(L.pscol.n);
+      L.level = b.level;
+      L.out_r0 = g.L.out_r0;
+      L.out_c0 = g.L.out_c0;
+      L.out_nr = g.L.out_nr;
+      L.out_nc = g.L.out_nc;
+      L.out_channels = P->channels;
+      L.rec_scale = (float)(1.0 / ((double)L.kr * L.kc) / ((double)L.mr * L.mc));
+      L.gb_scale = (float)(1.0 / ((double)L.sr * L.sc) / ((double)(L.mr / L.sr) * (L.mc / L.sc)));
+      L.gy_scale = (float)(1.0 / ((double)L.mr * L.mc));
+      L.gS = gout;
+      L.gS_stride = gs_stride;
+      L.tasks = ds->btasks + b.task_off;
+      L.ntasks = (int)b.tasks.size();
+      L.gather = ds->gather;
+      L.img0 = c0;
+      if (b.level == 2) {
+        L.src = u1;
+        L.src_stride = P->u1_elems;
+        L.gy = gy2;
+        L.gy_stride = P->gy2_elems;
+      } else if (b.level == 1) {
+        L.src = u0;
+        L.src_stride = P->u0_elems;
+        L.gy = gy1;
+        L.gy_stride = P->gy1_elems;
+        L.gyc = gy2;
+        L.gyc_stride = P->gy2_elems;
+      } else {
+        L.gy = u0;  // g_pad (real) over the input spectra, no longer needed
+        L.gy_stride = P->u0_elems;
+        L.gyc = gy1;
+        L.gyc_stride = P->gy1_elems;
+      }
+      if (b.has_ct) err = b.ct(L, F, nimg, stream);
+      else if (g.oned) err = launch_rt_bwd<false, true>(b, L, F, nimg, stream);
+      else if (L.cluster > 1) err = launch_rt_bwd<true, false>(b, L, F, nimg, stream);
+      else err = launch_rt_bwd<false, false>(b, L, F, nimg, stream);
+      if (err != cudaSuccess) return fail_cuda(err, "backward launch");
+    }
+    // 3. reflect-pad adjoint into g_x
+    const int total = nimg * P->img_M * P->img_N;
+    const int threads = 256;
+    const int blocks = (total + threads - 1) / threads;
+    reflect_pad_adjoint_kernel<<<blocks, threads, 0, stream>>>(
+        reinterpret_cast<const float*>(u0), 2 * P->u0_elems, P->Mp, P->Np, gx, P->img_M, P->img_N, P->pad_t,
+        P->pad_l, nimg, c0);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return fail_cuda(err, "reflect-pad adjoint");
+  }
+  return KYM_OK;
+}
+
 static void set_default_chunk(CascadePlan* P) {
   const double budget = 64.0 * 1024 * 1024;  // keep parent spectra L2-resident
   long long c = P->u1_elems ? (long long)(budget / (P->u1_elems * sizeof(float2))) : 1 << 20;
@@ -741,6 +1055,8 @@ extern "C" int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, in
   for (auto& g : P->groups) g.L.out_channels = P->channels;
   rc = finalize_groups(P);
   if (rc) goto fail;
+  rc = build_backward(P);
+  if (rc) goto fail;
   set_default_chunk(P);
   *out = h;
   return KYM_OK;
@@ -821,6 +1137,25 @@ extern "C" size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch) {
 namespace kym {
 CascadePlan* plan_of(const kym_s2d_plan* p) { return const_cast<CascadePlan*>(&p->p); }
 }  // namespace kym
+
+extern "C" int kym_s2d_set_backward_chunk(kym_s2d_plan* plan, int chunk) {
+  if (!plan || chunk < 1) return KYM_ERR_INVALID;
+  plan->p.bchunk = chunk;
+  return KYM_OK;
+}
+
+extern "C" size_t kym_s2d_backward_workspace_bytes(const kym_s2d_plan* plan, int batch) {
+  if (!plan || batch < 0) return 0;
+  return kym::backward_bytes(&plan->p, batch);
+}
+
+extern "C" int kym_s2d_backward(const kym_s2d_plan* plan, const float* x, const float* grad_out, float* grad_x,
+                                int batch, const float* const* filters, int n_filters, void* workspace,
+                                size_t workspace_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_backward(const_cast<CascadePlan*>(&plan->p), x, grad_out, grad_x, batch, filters, n_filters,
+                           workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
 
 extern "C" int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch,
                                const float* const* filters, int n_filters, void* workspace,
@@ -963,6 +1298,8 @@ extern "C" int kym_s1d_plan_create(int N_padded, int N_input, int pad_left, int 
   for (auto& g : P->groups) g.L.out_channels = P->channels;
   rc = finalize_groups(P);
   if (rc) goto fail;
+  rc = build_backward(P);
+  if (rc) goto fail;
   set_default_chunk(P);
   *out = h;
   return KYM_OK;
@@ -995,6 +1332,19 @@ extern "C" int kym_s1d_set_chunk(kym_s1d_plan* plan, int chunk) {
   if (!plan || chunk < 1) return KYM_ERR_INVALID;
   plan->p.chunk = chunk;
   return KYM_OK;
+}
+
+extern "C" size_t kym_s1d_backward_workspace_bytes(const kym_s1d_plan* plan, int batch) {
+  if (!plan || batch < 0) return 0;
+  return kym::backward_bytes(&plan->p, batch);
+}
+
+extern "C" int kym_s1d_backward(const kym_s1d_plan* plan, const float* x, const float* grad_out, float* grad_x,
+                                int batch, const float* const* filters, int n_filters, void* workspace,
+                                size_t workspace_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_backward(const_cast<CascadePlan*>(&plan->p), x, grad_out, grad_x, batch, filters, n_filters,
+                           workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int kym_s1d_forward(const kym_s1d_plan* plan, const float* x, float* out, int batch,

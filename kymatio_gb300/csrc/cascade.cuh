@@ -56,7 +56,8 @@ struct CascadeLaunch {
   long long out_stride;
   const Task* tasks;
   int ntasks;
-  int img0;  // first image of this chunk (for x/out offsets)
+  int img0;     // first image of this chunk (for x/out offsets)
+  int skip_s;   // 1: stop after storing the spectrum (backward recomputation)
 };
 
 }  // namespace kym

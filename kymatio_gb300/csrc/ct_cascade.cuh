@@ -145,6 +145,8 @@ __global__ void __launch_bounds__(NT, 1)
     for (int e = threadIdx.x; e < NLOC; e += NT) dst[e] = *at(e / MC, e % MC);
   }
 
+  if (L.skip_s) return;  // no remote shared-memory access follows the last cluster barrier
+
   // ---- low-pass: partial fold over local rows --------------------------------------
   constexpr int KSR = MR / SR, KSC = MC / SC;
   const float* phi = F.f[t.phi];

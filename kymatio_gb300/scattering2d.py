@@ -152,6 +152,23 @@ class Scattering2D(nn.Module):
                                            ws.data_ptr(), ws_bytes, stream), 'kym_s2d_forward')
         return out
 
+    def _backward_raw(self, x, grad):
+        """grad_x = J^T grad through kym_s2d_backward (hand-written adjoints)."""
+        plan = self._get_plan()
+        lib = _lib.load()
+        B = x.shape[0]
+        gx = torch.empty_like(x)
+        if B == 0:
+            return gx
+        with torch.cuda.device(x.device):
+            ptrs = self._filter_ptrs()
+            ws_bytes = lib.kym_s2d_backward_workspace_bytes(plan.h, B)
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=x.device)
+            stream = torch.cuda.current_stream(x.device).cuda_stream
+            _lib.check(lib.kym_s2d_backward(plan.h, x.data_ptr(), grad.data_ptr(), gx.data_ptr(), B, ptrs,
+                                            self._n_filters, ws.data_ptr(), ws_bytes, stream), 'kym_s2d_backward')
+        return gx
+
     def extra_repr(self):
         return 'J={}, shape={}, L={}, max_order={}, pre_pad={}, out_type={!r}'.format(
             self.J, self.shape, self.L, self.max_order, self.pre_pad, self.out_type)

@@ -17,7 +17,10 @@ on current scipy) and writes:
 * ``ref_cases_1d.npz`` -- the same for 1-D configurations (T local, global,
   zero, stride, the 8192-sample J=6 Q=(8,1) T=64 shape);
 * ``ref_bank_2d.npz`` -- the full 40x40 J=2 filter bank and per-filter
-  checksums of the 272x272 J=3 bank.
+  checksums of the 272x272 J=3 bank;
+* ``ref_grads.npz`` -- input gradients from the reference torch frontend's
+  autograd in float64 (x, upstream gradient g, d<g, S(x)>/dx) for 2-D and 1-D
+  configurations.
 
 Nothing at test time reads the reference; the tests read these files.
 """
@@ -112,5 +115,53 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, 'ref_bank_2d.npz'), **out)
 
 
+GRAD_2D = [
+    # name, J, (M, N), max_order, pre_pad, batch
+    ('g2_j2_32', 2, (32, 32), 2, False, 2),
+    ('g2_j4_128', 4, (128, 128), 2, False, 1),
+    ('g2_j3_64x48', 3, (64, 48), 2, False, 1),
+    ('g2_j1_31_prepad', 1, (31, 31), 2, True, 2),
+    ('g2_j3_40_order1', 3, (40, 40), 1, False, 2),
+]
+GRAD_1D = [
+    ('g1_j5_q4_n1024', dict(J=5, shape=1024, Q=4), 2),
+    ('g1_j6_q8_t64_n8192', dict(J=6, shape=8192, Q=(8, 1), T=64), 1),
+]
+
+
+def grads(ref_root):
+    sys.path.insert(0, ref_root)
+    import torch
+    from kymatio.scattering2d.frontend.torch_frontend import ScatteringTorch2D
+    from kymatio.scattering1d.frontend.torch_frontend import ScatteringTorch1D
+    torch.set_num_threads(os.cpu_count() or 1)
+    out = {}
+    for i, (name, J, shape, mo, pp, B) in enumerate(GRAD_2D):
+        S = ScatteringTorch2D(J, shape, max_order=mo, pre_pad=pp).double()
+        xs = (B, S._M_padded, S._N_padded) if pp else (B,) + shape
+        rng = np.random.default_rng(300 + i)
+        x = rng.random(xs).astype(np.float32)
+        xt = torch.from_numpy(x.astype(np.float64)).requires_grad_()
+        y = S(xt)
+        g = rng.standard_normal(tuple(y.shape)).astype(np.float32)
+        y.backward(torch.from_numpy(g.astype(np.float64)))
+        out[name + '/x'], out[name + '/g'], out[name + '/gx'] = x, g, xt.grad.numpy()
+    for i, (name, kw, B) in enumerate(GRAD_1D):
+        S = ScatteringTorch1D(**kw).double()
+        rng = np.random.default_rng(400 + i)
+        x = rng.standard_normal((B, kw['shape'])).astype(np.float32)
+        xt = torch.from_numpy(x.astype(np.float64)).requires_grad_()
+        y = S(xt)
+        g = rng.standard_normal(tuple(y.shape)).astype(np.float32)
+        y.backward(torch.from_numpy(g.astype(np.float64)))
+        out[name + '/x'], out[name + '/g'], out[name + '/gx'] = x, g, xt.grad.numpy()
+    meta = dict(g2=[dict(name=c[0], J=c[1], shape=list(c[2]), max_order=c[3], pre_pad=c[4]) for c in GRAD_2D],
+                g1=[dict(name=c[0], kwargs=c[1]) for c in GRAD_1D])
+    out['meta'] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, 'ref_grads.npz'), **out)
+
+
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    main(root)
+    grads(root)

@@ -95,3 +95,30 @@ def test_oracle_subsample_kat():
             for b in range(k):
                 z += x[:, a * m:(a + 1) * m, b * m:(b + 1) * m]
         assert np.allclose(y, z / k ** 2)
+
+
+def fd_grad_2d(oracle, x, g, pixels, h=1e-6):
+    """Central differences of <g, S(x)> in FP64 at the given pixel indices."""
+    out = []
+    for (b, i, j) in pixels:
+        xp = x.copy()
+        xm = x.copy()
+        xp[b, i, j] += h
+        xm[b, i, j] -= h
+        out.append((np.sum(g * oracle(xp)) - np.sum(g * oracle(xm))) / (2 * h))
+    return np.array(out)
+
+
+def test_oracle_fd_matches_reference_autograd():
+    """FP64 central differences through the oracle reproduce the reference
+    torch autograd gradient (pins the finite-difference check used on GPU)."""
+    d = _load('ref_grads.npz')
+    x = d['g2_j2_32/x'].astype(np.float64)
+    g = d['g2_j2_32/g'].astype(np.float64)
+    gx = d['g2_j2_32/gx']
+    S = Scattering2D(2, (32, 32))
+    rng = np.random.default_rng(9)
+    pix = [(int(rng.integers(2)), int(rng.integers(32)), int(rng.integers(32))) for _ in range(6)]
+    fd = fd_grad_2d(S, x, g, pix)
+    ref = np.array([gx[p] for p in pix])
+    assert np.abs(fd - ref).max() <= 1e-6 * max(1.0, np.abs(ref).max())
