@@ -382,7 +382,9 @@ static int make_group(CascadePlan* P, Group& g, int mr, int mc, int kr, int kc, 
   }
   static_assert(sizeof(int) == 4, "");
   if (g_use_ct) {
-    const CtEntry* e = ct_find(mr, mc, sr, sc, L.cluster, P->oned);
+    // image sources use fold 0; spectra fold kr x kr when square (2-D) or kc (1-D)
+    const int kf = src_image ? 0 : (P->oned ? kc : (kr == kc ? kr : -2));
+    const CtEntry* e = ct_find(mr, mc, sr, sc, L.cluster, P->oned, kf);
     if (e && e->smem <= max_smem) {
       g.has_ct = true;
       g.ct = *e;

@@ -3,9 +3,21 @@
 #include "ct_cascade.cuh"
 #include "bwd.cuh"
 KYM_CT_VARIANT(160, 160, 10, 10, 1, false, 512)
+KYM_CT_FOLD(160, 160, 10, 10, 1, false, 512, 0)
+KYM_CT_FOLD(160, 160, 10, 10, 1, false, 512, 1)
 KYM_CT_VARIANT(80, 80, 10, 10, 1, false, 512)
+KYM_CT_FOLD(80, 80, 10, 10, 1, false, 512, 0)
+KYM_CT_FOLD(80, 80, 10, 10, 1, false, 512, 1)
+KYM_CT_FOLD(80, 80, 10, 10, 1, false, 512, 2)
 KYM_CT_VARIANT(40, 40, 10, 10, 1, false, 512)
+KYM_CT_FOLD(40, 40, 10, 10, 1, false, 512, 0)
+KYM_CT_FOLD(40, 40, 10, 10, 1, false, 512, 1)
+KYM_CT_FOLD(40, 40, 10, 10, 1, false, 512, 2)
+KYM_CT_FOLD(40, 40, 10, 10, 1, false, 512, 4)
 KYM_CT_VARIANT(20, 20, 10, 10, 1, false, 512)
+KYM_CT_FOLD(20, 20, 10, 10, 1, false, 512, 2)
+KYM_CT_FOLD(20, 20, 10, 10, 1, false, 512, 4)
+KYM_CT_FOLD(20, 20, 10, 10, 1, false, 512, 8)
 KYM_BWD_VARIANT(160, 160, 10, 10, 1, false, 512)
 KYM_BWD_VARIANT(80, 80, 10, 10, 1, false, 512)
 KYM_BWD_VARIANT(40, 40, 10, 10, 1, false, 512)

@@ -13,13 +13,15 @@ using CtLauncher = cudaError_t (*)(const CascadeLaunch&, const FilterTable&, int
 struct CtEntry {
   int mr, mc, sr, sc, c;
   bool oned;
+  int kf;  // compile-time fold of the source: -1 runtime, 0 image source, k > 0 fold k x k
   size_t smem;
   CtLauncher fn;
 };
 
 // Registry of the instantiated variants (filled by static initialisers).
 void ct_register(const CtEntry& e);
-const CtEntry* ct_find(int mr, int mc, int sr, int sc, int c, bool oned);
+// Exact fold variant first, then the runtime-fold variant of the same size.
+const CtEntry* ct_find(int mr, int mc, int sr, int sc, int c, bool oned, int kf);
 
 __device__ __forceinline__ int ct_reflect(int i, int n) {
   if (n == 1) return 0;
@@ -39,7 +41,7 @@ struct CtGeom {
   static_assert(MR % SR == 0 && MC % SC == 0, "low-pass fold");
 };
 
-template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
 __global__ void __launch_bounds__(NT, 1)
     ct_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
   using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
@@ -61,13 +63,42 @@ __global__ void __launch_bounds__(NT, 1)
 
   // ---- load ------------------------------------------------------------------
   constexpr int NLOC = RL * MC;
-  if (L.src_image) {
+  if (KF == 0 || (KF < 0 && L.src_image)) {
     const float* x = L.x + (size_t)(L.img0 + img) * L.x_stride;
     for (int e = threadIdx.x; e < NLOC; e += NT) {
       const int u = e / MC, v = e % MC;
       const int iy = ONED ? 0 : ct_reflect(row0 + u - L.pad_t, L.img_M);
       const int ix = ct_reflect(v - L.pad_l, L.img_N);
       *at(u, v) = make_float2(__ldg(x + (size_t)iy * L.img_N + ix) * L.load_scale, 0.f);
+    }
+  } else if constexpr (KF > 0) {
+    // fold KF x KF aliases of src * psi, two adjacent columns per item
+    // (float4 / float2 loads: every offset is even because MC is even)
+    static_assert(MC % 2 == 0, "paired columns");
+    constexpr int KR = ONED ? 1 : KF;
+    constexpr int SCOLS = KF * MC;
+    const float4* src4 = reinterpret_cast<const float4*>(L.src + (size_t)img * L.src_stride + t.src_off);
+    const float2* psi2 = reinterpret_cast<const float2*>(F.f[t.psi]);
+    const float sc = L.load_scale;
+#pragma unroll 2
+    for (int e = threadIdx.x; e < NLOC / 2; e += NT) {
+      const int u = (2 * e) / MC, v = (2 * e) % MC;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int a = 0; a < KR; ++a) {
+#pragma unroll
+        for (int b = 0; b < KF; ++b) {
+          const size_t half = ((size_t)(row0 + u + a * MR) * SCOLS + v + b * MC) >> 1;
+          const float4 s4 = __ldg(src4 + half);
+          const float2 f2 = __ldg(psi2 + half);
+          acc.x = fmaf(s4.x, f2.x, acc.x);
+          acc.y = fmaf(s4.y, f2.x, acc.y);
+          acc.z = fmaf(s4.z, f2.y, acc.z);
+          acc.w = fmaf(s4.w, f2.y, acc.w);
+        }
+      }
+      *at(u, v) = make_float2(acc.x * sc, acc.y * sc);
+      *at(u, v + 1) = make_float2(acc.z * sc, acc.w * sc);
     }
   } else {
     const float2* src = L.src + (size_t)img * L.src_stride + t.src_off;
@@ -94,7 +125,7 @@ __global__ void __launch_bounds__(NT, 1)
   __syncthreads();
 
   const ct::RowLines<LD, ONED> rows{A};
-  if (L.modulus) {
+  if (KF != 0 && L.modulus) {
     ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, true);
     if constexpr (!ONED) {
       if constexpr (C > 1) {
@@ -201,10 +232,10 @@ __global__ void __launch_bounds__(NT, 1)
   }
 }
 
-template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
 cudaError_t ct_launch(const CascadeLaunch& L, const FilterTable& F, int nimg, cudaStream_t stream) {
   using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
-  auto kern = ct_cascade_kernel<MR, MC, SR, SC, C, ONED, NT>;
+  auto kern = ct_cascade_kernel<MR, MC, SR, SC, C, ONED, NT, KF>;
   static bool configured = false;  // per process; attributes are per function
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
@@ -230,15 +261,19 @@ cudaError_t ct_launch(const CascadeLaunch& L, const FilterTable& F, int nimg, cu
   return cudaLaunchKernelEx(&cfg, kern, L, F);
 }
 
-template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
 struct CtRegistrar {
   CtRegistrar() {
     using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
-    ct_register(CtEntry{MR, MC, SR, SC, C, ONED, G::smem, &ct_launch<MR, MC, SR, SC, C, ONED, NT>});
+    ct_register(CtEntry{MR, MC, SR, SC, C, ONED, KF, G::smem, &ct_launch<MR, MC, SR, SC, C, ONED, NT, KF>});
   }
 };
 
+// A size with a runtime fold (any source), plus compile-time folds.
 #define KYM_CT_VARIANT(MR, MC, SR, SC, C, ONED, NT) \
-  static ::kym::CtRegistrar<MR, MC, SR, SC, C, ONED, NT> kym_ct_reg_##MR##_##MC##_##SR##_##SC##_##C##_##ONED;
+  static ::kym::CtRegistrar<MR, MC, SR, SC, C, ONED, NT, -1> kym_ct_reg_##MR##_##MC##_##SR##_##SC##_##C##_##ONED;
+#define KYM_CT_FOLD(MR, MC, SR, SC, C, ONED, NT, KF) \
+  static ::kym::CtRegistrar<MR, MC, SR, SC, C, ONED, NT, KF>  \
+      kym_ct_regf_##MR##_##MC##_##SR##_##SC##_##C##_##ONED##_##KF;
 
 }  // namespace kym

@@ -20,11 +20,15 @@ void ct_register(const CtEntry& e) {
   ct_table().push_back(e);
 }
 
-const CtEntry* ct_find(int mr, int mc, int sr, int sc, int c, bool oned) {
+const CtEntry* ct_find(int mr, int mc, int sr, int sc, int c, bool oned, int kf) {
   std::lock_guard<std::mutex> lock(ct_mutex());
-  for (const CtEntry& e : ct_table())
-    if (e.mr == mr && e.mc == mc && e.sr == sr && e.sc == sc && e.c == c && e.oned == oned) return &e;
-  return nullptr;
+  const CtEntry* generic = nullptr;
+  for (const CtEntry& e : ct_table()) {
+    if (e.mr != mr || e.mc != mc || e.sr != sr || e.sc != sc || e.c != c || e.oned != oned) continue;
+    if (e.kf == kf) return &e;
+    if (e.kf < 0) generic = &e;
+  }
+  return generic;
 }
 
 }  // namespace kym
