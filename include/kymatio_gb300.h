@@ -116,6 +116,13 @@ int kym_s2d_backward(const kym_s2d_plan* plan, const float* x, const float* grad
 int kym_s2d_forward_noalloc(const kym_s2d_plan* plan, const float* x, float* out, int batch,
                             const float* const* filters, int n_filters, void* stream);
 
+/* Self-test of the tcgen05 split-precision GEMM (no reference counterpart):
+ * D (M x N) = A (M x K) * B (N x K)^T from bf16 hi/lo operands with FP32
+ * accumulation in tensor memory, one M=128 tile; M <= 128, N in
+ * {16, 32, 48, 64}, K <= 256.  *status gets bit 1 if the completion wait ran
+ * out (the result is then not written). */
+int kym_tc_selftest(const float* A, const float* B, float* D, int M, int N, int K, unsigned* status, void* stream);
+
 /* ------------------------------------------------------------------------
  * 1-D scattering, local averaging (replaces ScatteringBase1D.scattering with
  * average='local', kymatio/scattering1d/frontend/base_frontend.py:106-155,

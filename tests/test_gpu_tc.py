@@ -1,0 +1,33 @@
+"""tcgen05 split-precision GEMM self-test: bf16 hi/lo operands, FP32
+accumulation in tensor memory, against an FP64 product."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+torch = pytest.importorskip('torch')
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize('M,N,K', [(128, 32, 144), (100, 16, 68), (77, 64, 256), (128, 48, 40)])
+def test_tc_split_gemm(M, N, K):
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from kymatio_gb300 import _lib
+    lib = _lib.load()
+    dev = torch.device('cuda:0')
+    rng = np.random.default_rng(M * 7 + N + K)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((N, K)).astype(np.float32)
+    a, b = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+    d = torch.full((M, N), float('nan'), device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    _lib.check(lib.kym_tc_selftest(a.data_ptr(), b.data_ptr(), d.data_ptr(), M, N, K, status.data_ptr(),
+                                   torch.cuda.current_stream().cuda_stream), 'kym_tc_selftest')
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    ref = A.astype(np.float64) @ B.astype(np.float64).T
+    got = d.cpu().numpy()
+    assert np.isfinite(got).all()
+    # three-product bf16 split keeps ~16 mantissa bits per product
+    assert rel_l2(got, ref) < 2e-5, rel_l2(got, ref)
