@@ -187,6 +187,15 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def order_rel_l2(out, ref):
+    from oracle.scattering2d import order_slices
+    res = []
+    for sl in order_slices(J, L, 2):
+        a, b = out[:, sl].astype(np.float64), ref[:, sl]
+        res.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+    return res
+
+
 def run_ours(args, world, rank, local):
     import ctypes
     import torch
@@ -194,7 +203,8 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
     lib = _lib.load()
-    x_host = torch.from_numpy(grf_batch(BATCH, seed=2 + rank)).pin_memory()
+    x_np = grf_batch(BATCH, seed=2 + rank)
+    x_host = torch.from_numpy(x_np).pin_memory()
     x = x_host.to(dev)
     S = Scattering2D(J, (SIDE, SIDE), L=L).to(dev)
     if args.chunk:
@@ -205,7 +215,7 @@ def run_ours(args, world, rank, local):
     for g in range(ngroups):
         v = [ctypes.c_int() for _ in range(6)]
         lib.kym_s2d_group_info(plan.h, g, *[ctypes.byref(i) for i in v])
-        ginfo.append([i.value for i in v])
+        ginfo.append([i.value for i in v] + [lib.kym_s2d_group_uses_tc(plan.h, g)])
     chunk = lib.kym_s2d_get_chunk(plan.h)
     n_chunks = -(-BATCH // min(chunk, BATCH))
     launches_per_step = sum(1 if gi[0] == 0 else n_chunks for gi in ginfo)
@@ -213,12 +223,19 @@ def run_ours(args, world, rank, local):
     ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, BATCH)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     ptrs = S._filter_ptrs()
+    lr, lc = S._lowpass_ptrs()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
     stream = torch.cuda.current_stream(dev)
     gms = (ctypes.c_float * ngroups)()
 
-    def step(timed_groups):
-        if timed_groups:
+    def step(form, timed_groups):
+        g = gms if timed_groups else None
+        ng = ngroups if timed_groups else 0
+        if form == 'tc':
+            _lib.check(lib.kym_s2d_forward_tc(plan.h, x.data_ptr(), out.data_ptr(), BATCH, ptrs, S._n_filters, lr, lc,
+                                              J, ws.data_ptr(), ws_bytes, S._tc_status.data_ptr(),
+                                              stream.cuda_stream, g, ng), 'forward_tc')
+        elif timed_groups:
             _lib.check(lib.kym_s2d_forward_timed(plan.h, x.data_ptr(), out.data_ptr(), BATCH, ptrs, S._n_filters,
                                                  ws.data_ptr(), ws_bytes, stream.cuda_stream, gms, ngroups),
                        'forward_timed')
@@ -226,41 +243,52 @@ def run_ours(args, world, rank, local):
             _lib.check(lib.kym_s2d_forward(plan.h, x.data_ptr(), out.data_ptr(), BATCH, ptrs, S._n_filters,
                                            ws.data_ptr(), ws_bytes, stream.cuda_stream), 'forward')
 
-    for _ in range(args.warmup):
-        step(False)
-    torch.cuda.synchronize()
-    # ---- device-timed region: per-step events, L2 flushed between steps ----
+    def measure(form):
+        for _ in range(args.warmup):
+            step(form, False)
+        torch.cuda.synchronize()
+        barrier(world)
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(form, False)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        barrier(world)
+        gtot = np.zeros(ngroups)
+        for _ in range(args.steps):
+            flush.zero_()
+            step(form, True)
+            gtot += np.array([gms[i] for i in range(ngroups)])
+        return max_over_ranks(sum(times) / len(times), world), gtot / args.steps
+
+    # precision of both forms on two images vs the FP64 oracle
+    prec = {}
+    if rank == 0 and not args.no_cpu:
+        from oracle.scattering2d import Scattering2D as Oracle
+        ref = Oracle(J, (SIDE, SIDE), L=L)(x_np[:2].astype(np.float64))
+        for form in ('plain', 'tc'):
+            step(form, False)
+            torch.cuda.synchronize()
+            prec[form] = order_rel_l2(out[:2].cpu().numpy(), ref)
     sampler = ClockSampler(local)
     sampler.start()
-    barrier(world)
-    torch.cuda.synchronize()
-    step_ms = []
-    group_tot = np.zeros(ngroups)
-    for _ in range(args.steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step(False)
-        e1.record(stream)
-        e1.synchronize()
-        step_ms.append(e0.elapsed_time(e1))
-    torch.cuda.synchronize()
-    barrier(world)
-    # per-launch kernel durations of every group (same stream, same workload)
-    for _ in range(args.steps):
-        flush.zero_()
-        step(True)
-        group_tot += np.array([gms[i] for i in range(ngroups)])
+    t_plain, g_plain = measure('plain')
+    t_tc, g_tc = measure('tc')
     clocks = sampler.stop()
-    t_step = max_over_ranks(sum(step_ms) / len(step_ms), world)
-    value = BATCH * world / (t_step / 1e3)
-    # ---- end to end through the public API: pinned host in, host out -------
+    tc_status = S.tensor_core_status()
+    value = BATCH * world / (t_tc / 1e3)
+    value_plain = BATCH * world / (t_plain / 1e3)
+    # ---- end to end through the public API (tensor-core form): pinned host in, host out
+    S.tensor_cores = True
     out_host = torch.empty((BATCH, S._channels) + S._out_hw, dtype=torch.float32).pin_memory()
     for _ in range(max(1, args.warmup)):
         out_host.copy_(S(x_host.to(dev, non_blocking=True)), non_blocking=True)
     torch.cuda.synchronize()
     barrier(world)
-    t0 = time.perf_counter()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -269,7 +297,6 @@ def run_ours(args, world, rank, local):
         out_host.copy_(S(x_host.to(dev, non_blocking=True)), non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
-    flush_ms = 0.0
     fe0, fe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     fe0.record(stream)
     for _ in range(args.steps):
@@ -279,23 +306,17 @@ def run_ours(args, world, rank, local):
     flush_ms = fe0.elapsed_time(fe1)
     e2e_ms = max_over_ranks((e0.elapsed_time(e1) - flush_ms) / args.steps, world)
     e2e = BATCH * world / (e2e_ms / 1e3)
-    # ---- roofline of the dominant group -------------------------------------
-    per_launch = []
-    for g, gi in enumerate(ginfo):
-        nl = 1 if gi[0] == 0 else n_chunks
-        per_launch.append(group_tot[g] / args.steps / nl)
-    dom = int(np.argmax(group_tot))
-    lvl, ntasks, rows, cols, fold, cl = ginfo[dom]
+    # ---- roofline of the dominant launch group of the tensor-core form -----------
+    per_launch = [g_tc[g] / (1 if gi[0] == 0 else n_chunks) for g, gi in enumerate(ginfo)]
+    dom = int(np.argmax(g_tc))
+    lvl, ntasks, rows, cols, fold, cl, uses_tc = ginfo[dom]
     imgs_per_launch = BATCH if lvl == 0 else min(chunk, BATCH)
-    # algorithmic bytes of one launch of that group: per task and image it
-    # reads the parent spectrum and the wavelet (fold^2 * rows*cols complex +
-    # real), the low-pass filter (rows*cols real) and writes its output channel
     side_out = SIDE // 2 ** J
     if lvl == 0:
         bytes_launch = imgs_per_launch * (4 * SIDE * SIDE + 8 * rows * cols + 4 * side_out ** 2)
     else:
         src = fold * fold * rows * cols
-        spill_w = 8 * rows * cols if (lvl == 1 and rows > (272 >> (J - 1))) else 0
+        spill_w = 8 * rows * cols if (lvl == 1 and not uses_tc and rows > (272 >> (J - 1))) else 0
         bytes_launch = imgs_per_launch * ntasks * (8 * src + 4 * side_out ** 2 + spill_w) + \
             ntasks * (4 * src + 4 * rows * cols)
     dur_s = per_launch[dom] / 1e3
@@ -324,23 +345,30 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         line = {
             'metric': METRIC, 'value': value, 'unit': 'img/s', 'n_gpus': world, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': t_step, 'higher_is_better': True, 'scaling': 'weak',
+            'warmup': args.warmup, 'ms_per_step': t_tc, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': 'Scattering2D J=3 L=8 max_order=2, 256x256 GRF float32, plain FP32 fused path',
+            'config': {'workload': 'Scattering2D J=3 L=8 max_order=2, 256x256 GRF float32, tensor-core '
+                                   'split-precision form (tcgen05 bf16 hi/lo, fp32 accumulate)',
                        'global_batch': BATCH * world, 'per_gpu_batch': BATCH, 'chunk': chunk,
                        'l2': 'flushed (256 MB write) between timed steps', 'parallelism': 'replicas x%d' % world},
+            'plain_fp32': {'value': value_plain, 'unit': 'img/s', 'ms_per_step': t_plain,
+                           'rel_l2_vs_fp64': prec.get('plain'),
+                           'group_ms_per_step': [round(v, 4) for v in g_plain]},
+            'tc_vs_plain': value / value_plain,
+            'rel_l2_vs_fp64': prec.get('tc'), 'rel_l2_orders': ['S0', 'S1', 'S2'],
+            'tc_status': tc_status,
             'e2e': {'value': e2e, 'unit': 'img/s', 'h2d_bytes_per_step': int(x_host.numel() * 4),
                     'd2h_bytes_per_step': int(out_host.numel() * 4)},
             'gpu_launches': launches_per_step * args.steps,
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s',
                          'frac': achieved / hbm_peak, 'traffic': traffic,
-                         'kernel': 'cascade group %d (level %d, %dx%d, fold %d, cluster %d, %d tasks)'
-                                   % (dom, lvl, rows, cols, fold, cl, ntasks),
+                         'kernel': 'cascade group %d (level %d, %dx%d, fold %d, cluster %d, %d tasks%s)'
+                                   % (dom, lvl, rows, cols, fold, abs(cl), ntasks, ', tensor-core' if uses_tc else ''),
                          'kernel_ms_per_launch': per_launch[dom],
                          'peak_source': 'measured' if 'hbm_gbs' in peaks else 'fallback'},
             'fp32_fft': {'gflop_per_img_5nlogn': flops_img / 1e9,
-                         'achieved_tflops': flops_img * value / world / 1e12},
-            'group_ms_per_step': [round(v / args.steps, 4) for v in group_tot],
+                         'achieved_tflops_plain': flops_img * value_plain / world / 1e12},
+            'group_ms_per_step': [round(v, 4) for v in g_tc],
             'clocks': clocks,
             'cpu_baseline': cpu,
         }

@@ -83,6 +83,22 @@ int kym_s2d_forward_timed(const kym_s2d_plan* plan, const float* x, float* out, 
 int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
                     int n_filters, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Tensor-core split-precision forward (the reference has no counterpart; it
+ * computes the same transform as kym_s2d_forward).  Every childless path
+ * (order 2, and the last order-1 scale) runs its low-pass branch as the
+ * separable product S = T_r U T_c^T: U T_c^T on tcgen05 from BF16 hi/lo
+ * operands with FP32 accumulation, T_r (.) in FP32.  lowpass_rows[j] /
+ * lowpass_cols[j] are the float32 factors (out_rows x M_padded/2^j and
+ * out_cols x N_padded/2^j) of low-pass filter j; *status (device) gets bit 1
+ * if a tensor-core completion wait ran out.  group_ms/max_groups as in
+ * kym_s2d_forward_timed (pass NULL/0 to skip timing). */
+int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int batch, const float* const* filters,
+                       int n_filters, const float* const* lowpass_rows, const float* const* lowpass_cols,
+                       int n_lowpass, void* workspace, size_t workspace_bytes, unsigned* status, void* stream,
+                       float* group_ms, int max_groups);
+/* 1 if launch group `group` runs a tensor-core variant in kym_s2d_forward_tc. */
+int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);
+
 /* Hand-written backward: grad_x (batch, M, N) = (d forward / d x)^T grad_out,
  * grad_out shaped like the forward's output.  Replaces torch autograd through
  * the reference op surface (unpad, irfft, subsample_fourier, cdgmm, rfft,

@@ -17,6 +17,7 @@
 #include "cascade.cuh"
 #include "ct_cascade.cuh"
 #include "bwd.cuh"
+#include "tc_cascade.cuh"
 #include "plan_util.h"
 #include "errors.h"
 
@@ -221,6 +222,9 @@ struct Group {
   CascadeLaunch L;       // pointers filled at launch
   bool has_ct = false;   // a compile-time specialised variant exists
   CtEntry ct{};
+  bool has_tc = false;   // a tensor-core variant exists (childless tasks only)
+  size_t tc_smem = 0;
+  TcLauncher tc = nullptr;
   std::vector<Task> tasks;
   size_t task_off = 0;   // offset into the device task array
   size_t smem = 0;
@@ -432,6 +436,8 @@ static cudaError_t launch_group(const Group& g, const CascadeLaunch& L, const Fi
 // runs the input stage chunk by chunk (the workspace then holds the input
 // spectra of one chunk only).
 struct RunArgs {
+  const LowpassTable* lp = nullptr;  // non-null: tensor-core form for the groups that have one
+  unsigned* status = nullptr;
   const DeviceState* ds = nullptr;
   float2* u0 = nullptr;
   float2* u1 = nullptr;
@@ -523,7 +529,8 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           cudaEventCreate(&e1);
           cudaEventRecord(e0, stream);
         }
-        if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
+        if (a.lp && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
+        else if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
         else if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
         else if (Li.cluster > 1) err = launch_group<true, false>(g, Li, F, ni, stream);
         else err = launch_group<false, false>(g, Li, F, ni, stream);
@@ -556,7 +563,8 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
 
 static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
                     int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
-                    float* group_ms = nullptr, int max_groups = 0) {
+                    float* group_ms = nullptr, int max_groups = 0, const LowpassTable* lp = nullptr,
+                    unsigned* status = nullptr) {
   if (!P || !x || !out || batch < 0) {
     set_error_message("forward", "null plan, input or output");
     return KYM_ERR_INVALID;
@@ -580,7 +588,27 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   a.chunk = chunk;
   a.group_ms = group_ms;
   a.max_groups = max_groups;
+  a.lp = lp;
+  a.status = status;
   return run_core(P, x, out, batch, F, a, stream);
+}
+
+// Tensor-core variants for the childless groups (2-D, one CTA per task).
+static void attach_tc(CascadePlan* P) {
+  for (Group& g : P->groups) {
+    g.has_tc = false;
+    if (P->oned || g.level == 0 || g.L.cluster != 1 || g.L.kr != g.L.kc) continue;
+    bool childless = true;
+    for (const Task& t : g.tasks) childless &= t.dst_off < 0;
+    if (!childless) continue;
+    size_t smem = 0;
+    TcLauncher fn = nullptr;
+    if (tc_find(g.L.mr, g.L.mc, g.L.out_nr, g.L.out_nc, g.L.kr, &smem, &fn) && smem <= max_dynamic_smem()) {
+      g.has_tc = true;
+      g.tc_smem = smem;
+      g.tc = fn;
+    }
+  }
 }
 
 // Forward whose tables and workspace live in a caller-provided device buffer
@@ -1059,6 +1087,7 @@ extern "C" int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, in
   if (rc) goto fail;
   rc = build_backward(P);
   if (rc) goto fail;
+  attach_tc(P);
   set_default_chunk(P);
   *out = h;
   return KYM_OK;
@@ -1127,6 +1156,31 @@ extern "C" int kym_s2d_forward_timed(const kym_s2d_plan* plan, const float* x, f
   if (!plan || !group_ms || max_groups < 1) return KYM_ERR_INVALID;
   return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
                        workspace_bytes, static_cast<cudaStream_t>(stream), group_ms, max_groups);
+}
+
+extern "C" int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int batch,
+                                  const float* const* filters, int n_filters, const float* const* lowpass_rows,
+                                  const float* const* lowpass_cols, int n_lowpass, void* workspace,
+                                  size_t workspace_bytes, unsigned* status, void* stream, float* group_ms,
+                                  int max_groups) {
+  if (!plan || !lowpass_rows || !lowpass_cols || !status || n_lowpass < 1 || n_lowpass > kym::kMaxLowpass) {
+    kym::set_error_message("forward_tc", "needs the separable low-pass factors and a status word");
+    return KYM_ERR_INVALID;
+  }
+  kym::LowpassTable lp;
+  std::memset(&lp, 0, sizeof(lp));
+  for (int i = 0; i < n_lowpass; ++i) {
+    lp.r[i] = lowpass_rows[i];
+    lp.c[i] = lowpass_cols[i];
+  }
+  return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
+                       workspace_bytes, static_cast<cudaStream_t>(stream), group_ms, group_ms ? max_groups : 0, &lp,
+                       status);
+}
+
+extern "C" int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group) {
+  if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
+  return plan->p.groups[group].has_tc ? 1 : 0;
 }
 
 extern "C" size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch) {
@@ -1302,6 +1356,7 @@ extern "C" int kym_s1d_plan_create(int N_padded, int N_input, int pad_left, int 
   if (rc) goto fail;
   rc = build_backward(P);
   if (rc) goto fail;
+  attach_tc(P);
   set_default_chunk(P);
   *out = h;
   return KYM_OK;

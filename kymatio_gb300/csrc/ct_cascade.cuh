@@ -41,26 +41,17 @@ struct CtGeom {
   static_assert(MR % SR == 0 && MC % SC == 0, "low-pass fold");
 };
 
-template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
-__global__ void __launch_bounds__(NT, 1)
-    ct_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
-  using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
-  constexpr int RL = G::RL, LD = G::LD, LDB = G::LDB;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* A = reinterpret_cast<float2*>(smem_raw);
-  float2* B = A + RL * LD;
-  int rank = 0;
-  if constexpr (C > 1) rank = static_cast<int>(cg::this_cluster().block_rank());
-  const int task_id = blockIdx.x / C;
-  const int img = blockIdx.y;
-  const Task t = L.tasks[task_id];
-  const int row0 = rank * RL;
-
+// Load phase of a task: the reflect-padded image (KF == 0), or the fold of
+// src * psi over KF x KF aliases (KF > 0, paired float4 loads), or a
+// runtime fold (KF < 0).  Writes the local rows of the work array A.
+template <int MR, int MC, int C, bool ONED, int NT, int KF, int LD>
+__device__ __forceinline__ void ct_load(float2* A, const CascadeLaunch& L, const FilterTable& F, const Task& t,
+                                        int img, int row0) {
+  constexpr int RL = MR / C;
   auto at = [&](int u, int v) -> float2* {
     if constexpr (ONED) return A + (v + (v >> 4));
     else return A + u * LD + v;
   };
-
   // ---- load ------------------------------------------------------------------
   constexpr int NLOC = RL * MC;
   if (KF == 0 || (KF < 0 && L.src_image)) {
@@ -122,7 +113,31 @@ __global__ void __launch_bounds__(NT, 1)
       *at(u, v) = cscale(acc, L.load_scale);
     }
   }
+}
+
+template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
+__global__ void __launch_bounds__(NT, 1)
+    ct_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
+  using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
+  constexpr int RL = G::RL, LD = G::LD, LDB = G::LDB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* A = reinterpret_cast<float2*>(smem_raw);
+  float2* B = A + RL * LD;
+  int rank = 0;
+  if constexpr (C > 1) rank = static_cast<int>(cg::this_cluster().block_rank());
+  const int task_id = blockIdx.x / C;
+  const int img = blockIdx.y;
+  const Task t = L.tasks[task_id];
+  const int row0 = rank * RL;
+
+  auto at = [&](int u, int v) -> float2* {
+    if constexpr (ONED) return A + (v + (v >> 4));
+    else return A + u * LD + v;
+  };
+
+  ct_load<MR, MC, C, ONED, NT, KF, LD>(A, L, F, t, img, row0);
   __syncthreads();
+  constexpr int NLOC = RL * MC;
 
   const ct::RowLines<LD, ONED> rows{A};
   if (KF != 0 && L.modulus) {

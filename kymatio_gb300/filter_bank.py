@@ -211,3 +211,31 @@ def border_indices(log2_T, J, i0, i1):
         start[j] = start[j - 1] // 2 + start[j - 1] % 2
         end[j] = end[j - 1] // 2 + end[j - 1] % 2
     return start, end
+
+
+# ---------------------------------------------------------------------------
+# Separable low-pass factors (tensor-core form)
+# ---------------------------------------------------------------------------
+
+def separable_lowpass(phi_level, out_r0, out_nr, out_c0, out_nc, ks_r, ks_c):
+    """Factors T_r (out_nr x m_r), T_c (out_nc x m_c) with
+
+        unpad(Re IFFT2_s(fold_ks(FFT2_m(U) * phi_level))) = T_r U T_c^T
+
+    for real U.  phi_level (real, m_r x m_c) is the periodised Gaussian of the
+    bank, a rank-one outer product u v^T up to float32 rounding (FP64 SVD);
+    T_r[p, x] = h_u[((p + out_r0) ks_r - x) mod m_r] with h_u = IFFT(u).
+    Returns (T_r, T_c, relative residual of the rank-one fit)."""
+    f = np.asarray(phi_level, np.float64)
+    U, s, Vt = np.linalg.svd(f)
+    u, v = U[:, 0] * np.sqrt(s[0]), Vt[0] * np.sqrt(s[0])
+    if u.sum() < 0:
+        u, v = -u, -v
+    resid = float(np.linalg.norm(f - np.outer(u, v)) / np.linalg.norm(f))
+    hu, hv = np.fft.ifft(u).real, np.fft.ifft(v).real
+    mr, mc = f.shape
+    P = np.arange(out_r0, out_r0 + out_nr)[:, None]
+    Q = np.arange(out_c0, out_c0 + out_nc)[:, None]
+    Tr = hu[(P * ks_r - np.arange(mr)[None, :]) % mr]
+    Tc = hv[(Q * ks_c - np.arange(mc)[None, :]) % mc]
+    return Tr, Tc, resid

@@ -13,7 +13,7 @@ import torch
 import torch.nn as nn
 
 from . import _lib
-from .filter_bank import filter_bank_2d, padded_size_2d
+from .filter_bank import filter_bank_2d, padded_size_2d, separable_lowpass
 
 
 class Scattering2D(nn.Module):
@@ -21,9 +21,12 @@ class Scattering2D(nn.Module):
 
     Parameters follow kymatio.torch.Scattering2D: J (log2 scale), shape (M, N),
     L (orientations, default 8), max_order (1 or 2), pre_pad (input already
-    padded to the padded size), backend (accepted for signature
-    compatibility; the engine is always the GB300 cascade), out_type
-    ('array' or 'list').
+    padded to the padded size), backend, out_type ('array' or 'list').
+
+    backend='torch' (default) runs the plain FP32 cascade.  backend='torch_tc'
+    selects the tensor-core split-precision form: paths without children
+    compute their low-pass branch as a separable product on tcgen05 (BF16
+    hi/lo operands, FP32 accumulation); ``tensor_cores`` toggles it later.
     """
 
     def __init__(self, J, shape, L=8, max_order=2, pre_pad=False, backend='torch', out_type='array'):
@@ -57,7 +60,16 @@ class Scattering2D(nn.Module):
         self._n_filters = n
         self._plan = None
         self._ptr_cache = (None, None)
+        self._lp_cache = (None, None, None)
         self._meta = self._path_meta()
+        self.tensor_cores = isinstance(backend, str) and backend in ('torch_tc', 'torch_split')
+        # separable factors of every low-pass level (non-persistent: derived from tensor{j})
+        s_r, s_c = self._M_padded // 2 ** self.J, self._N_padded // 2 ** self.J
+        for j, lv in enumerate(self.phi['levels']):
+            Tr, Tc, _ = separable_lowpass(lv, 1, s_r - 2, 1, s_c - 2, 2 ** (self.J - j), 2 ** (self.J - j))
+            self.register_buffer('lowpass_r' + str(j), torch.from_numpy(Tr.astype('float32')), persistent=False)
+            self.register_buffer('lowpass_c' + str(j), torch.from_numpy(Tc.astype('float32')), persistent=False)
+        self.register_buffer('_tc_status', torch.zeros(1, dtype=torch.int32), persistent=False)
 
     # -- plan ---------------------------------------------------------------
     def _get_plan(self):
@@ -135,8 +147,27 @@ class Scattering2D(nn.Module):
             return S
         return [dict(m, coef=S[..., c, :, :]) for c, m in enumerate(self._meta)]
 
+    def _lowpass_ptrs(self):
+        r = [getattr(self, 'lowpass_r' + str(j)) for j in range(self.J)]
+        c = [getattr(self, 'lowpass_c' + str(j)) for j in range(self.J)]
+        key = tuple(t.data_ptr() for t in r + c)
+        if self._lp_cache[0] != key:
+            for t in r + c:
+                if not t.is_cuda or t.dtype != torch.float32 or not t.is_contiguous():
+                    raise TypeError('The low-pass factors must be contiguous float32 CUDA tensors.')
+            self._lp_cache = (key, _lib.ptr_array([t.data_ptr() for t in r]), _lib.ptr_array([t.data_ptr() for t in c]))
+        return self._lp_cache[1], self._lp_cache[2]
+
+    def tensor_core_status(self, reset=True):
+        """Non-zero when a tensor-core completion wait ran out (outputs are NaN then)."""
+        v = int(self._tc_status.item())
+        if reset:
+            self._tc_status.zero_()
+        return v
+
     def _forward_raw(self, x):
-        """(B, M, N) float32 CUDA -> (B, C, m, n) through kym_s2d_forward."""
+        """(B, M, N) float32 CUDA -> (B, C, m, n) through kym_s2d_forward (or
+        kym_s2d_forward_tc with tensor_cores)."""
         plan = self._get_plan()
         lib = _lib.load()
         B = x.shape[0]
@@ -148,8 +179,15 @@ class Scattering2D(nn.Module):
             ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, B)
             ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=x.device)
             stream = torch.cuda.current_stream(x.device).cuda_stream
-            _lib.check(lib.kym_s2d_forward(plan.h, x.data_ptr(), out.data_ptr(), B, ptrs, self._n_filters,
-                                           ws.data_ptr(), ws_bytes, stream), 'kym_s2d_forward')
+            if self.tensor_cores:
+                lr, lc = self._lowpass_ptrs()
+                _lib.check(lib.kym_s2d_forward_tc(plan.h, x.data_ptr(), out.data_ptr(), B, ptrs, self._n_filters,
+                                                  lr, lc, self.J, ws.data_ptr(), ws_bytes,
+                                                  self._tc_status.data_ptr(), stream, None, 0),
+                           'kym_s2d_forward_tc')
+            else:
+                _lib.check(lib.kym_s2d_forward(plan.h, x.data_ptr(), out.data_ptr(), B, ptrs, self._n_filters,
+                                               ws.data_ptr(), ws_bytes, stream), 'kym_s2d_forward')
         return out
 
     def _backward_raw(self, x, grad):

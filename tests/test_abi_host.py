@@ -90,3 +90,25 @@ def test_product_bank_checksums_272():
                     for lv in levels])
     assert got.shape == d.shape
     assert np.array_equal(got, d)
+
+
+@pytest.mark.parametrize('M,J', [(256, 3), (32, 2), (128, 4), (64, 3)])
+def test_separable_lowpass_identity(M, J):
+    """T_r U T_c^T reproduces unpad(Re IFFT2(fold(FFT2(U) phi))) in FP64 for
+    every low-pass level, and phi is rank one to float32 rounding."""
+    from kymatio_gb300.filter_bank import filter_bank_2d, padded_size_2d, separable_lowpass
+    Mp, Np = padded_size_2d(M, M, J)
+    phi, _ = filter_bank_2d(Mp, Np, J, 8)
+    s = Mp // 2 ** J
+    rng = np.random.default_rng(J)
+    for j, lv in enumerate(phi):
+        m = Mp >> j
+        ks = m // s
+        Tr, Tc, resid = separable_lowpass(lv, 1, s - 2, 1, s - 2, ks, ks)
+        assert resid < 1e-6
+        U = rng.random((m, m))
+        Z = np.fft.fft2(U) * lv
+        B = Z.reshape(ks, s, ks, s).mean(axis=(0, 2))
+        ref = np.fft.ifft2(B).real[1:-1, 1:-1]
+        got = Tr @ U @ Tc.T
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-6
