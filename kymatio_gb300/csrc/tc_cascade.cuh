@@ -52,6 +52,14 @@ __global__ void __launch_bounds__(NT, 1)
                       const __grid_constant__ LowpassTable LP, unsigned* status) {
   using G = TcGeom<MR, MC, NOUTC>;
   constexpr int LD = G::LD, KP = G::KP, NP = G::NP, MT = G::MT, TLD = G::TLD;
+  // M tile mt covers rows [tile_row0, tile_row0 + 128); the last tile of a
+  // height above 128 is shifted back so that it ends at the last row group
+  // (overlapping rows are computed twice, identically)
+  auto tile_row0 = [](int mt) -> int {
+    constexpr int MR8 = (MR + 7) / 8 * 8;
+    const int r = mt * 128;
+    return (MR > 128 && r + 128 > MR8) ? MR8 - 128 : r;
+  };
   extern __shared__ __align__(1024) unsigned char smem[];
   float2* A = reinterpret_cast<float2*>(smem);
   unsigned char* aop = smem;
@@ -75,50 +83,77 @@ __global__ void __launch_bounds__(NT, 1)
   __syncthreads();
   ct::fft_lines<MC, MR, NT>(ct::RowLines<LD, false>{A}, 0, L.prow.tw, true);
   ct::fft_lines<MR, MC, NT>(ct::ColLines<LD>{A}, 0, L.pcol.tw, true);
-  constexpr int NLOC = MR * MC;
-  constexpr int PER = (NLOC + NT - 1) / NT;
-  float u[PER];
+  // Operand A = U in core-matrix layout, written as 16-byte chunks: item g
+  // covers row r and the 8 columns 8c..8c+7 (one core-matrix row); eight
+  // consecutive items are the 8 rows of one core matrix (128 contiguous
+  // bytes).  Rows beyond MR are never written: they only feed output rows
+  // that are discarded.  Columns beyond MC are zero.
+  constexpr int G8 = KP / 8;              // chunks per row
+  constexpr int MR8 = (MR + 7) / 8 * 8;   // rows rounded to whole core matrices
+  constexpr int NIT = MR8 * G8;
+  constexpr int PER = (NIT + NT - 1) / NT;
+  uint4 hi4[PER], lo4[PER];
 #pragma unroll
   for (int i = 0; i < PER; ++i) {
-    const int e = tid + i * NT;
-    u[i] = 0.f;
-    if (e < NLOC) {
-      const float2 z = A[(e / MC) * LD + (e % MC)];
-      u[i] = sqrtf(fmaf(z.x, z.x, z.y * z.y));
+    const int g = tid + i * NT;
+    hi4[i] = make_uint4(0, 0, 0, 0);
+    lo4[i] = make_uint4(0, 0, 0, 0);
+    if (g < NIT) {
+      const int r = (g / 8) % (MR8 / 8) * 8 + (g % 8);  // 8 consecutive items = 8 rows
+      const int c = g / MR8;
+      uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
+      if (r < MR) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int k = 8 * c + q;
+          float uv = 0.f;
+          if (k < MC) {
+            const float2 z = A[r * LD + k];
+            uv = sqrtf(fmaf(z.x, z.x, z.y * z.y));
+          }
+          __nv_bfloat16 bh, bl;
+          tc::split_bf16(uv, bh, bl);
+          h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
+          l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
+        }
+      }
+      hi4[i] = make_uint4(h[0], h[1], h[2], h[3]);
+      lo4[i] = make_uint4(l[0], l[1], l[2], l[3]);
     }
   }
   __syncthreads();  // the FFT array is dead from here on; its space holds the operands
-
-  // ---- operands: A = U (MT*128 x KP, rows/cols beyond MR/MC zero), B = T_c --------
   const size_t a_half = (size_t)MT * 128 * KP * 2;
-  for (int e = tid; e < MT * 128 * KP; e += NT) {
-    const int r = e / KP, k = e % KP;
-    if (r < MR && k < MC) continue;  // written from registers below
-    const uint32_t off = tc::kmajor_offset(r, k, KP);
-    *reinterpret_cast<uint16_t*>(aop + off) = 0;
-    *reinterpret_cast<uint16_t*>(aop + a_half + off) = 0;
-  }
 #pragma unroll
   for (int i = 0; i < PER; ++i) {
-    const int e = tid + i * NT;
-    if (e < NLOC) {
-      const uint32_t off = tc::kmajor_offset(e / MC, e % MC, KP);
-      __nv_bfloat16 h, l;
-      tc::split_bf16(u[i], h, l);
-      *reinterpret_cast<__nv_bfloat16*>(aop + off) = h;
-      *reinterpret_cast<__nv_bfloat16*>(aop + a_half + off) = l;
+    const int g = tid + i * NT;
+    if (g < NIT) {
+      const int r = (g / 8) % (MR8 / 8) * 8 + (g % 8);
+      const int c = g / MR8;
+      const uint32_t off = tc::kmajor_offset(r, 8 * c, KP);
+      *reinterpret_cast<uint4*>(aop + off) = hi4[i];
+      *reinterpret_cast<uint4*>(aop + a_half + off) = lo4[i];
     }
   }
+  // operand B = T_c (NP x KP, rows beyond NOUTC and columns beyond MC zero)
   const float* tcm = LP.c[t.phi];
   const size_t b_half = (size_t)NP * KP * 2;
-  for (int e = tid; e < NP * KP; e += NT) {
-    const int r = e / KP, k = e % KP;
-    const float v = (r < NOUTC && k < MC) ? __ldg(tcm + r * MC + k) : 0.f;
-    __nv_bfloat16 h, l;
-    tc::split_bf16(v, h, l);
-    const uint32_t off = tc::kmajor_offset(r, k, KP);
-    *reinterpret_cast<__nv_bfloat16*>(bop + off) = h;
-    *reinterpret_cast<__nv_bfloat16*>(bop + b_half + off) = l;
+  for (int g = tid; g < NP * G8; g += NT) {
+    const int r = g % NP, c = g / NP;
+    uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
+    if (r < NOUTC) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = 8 * c + q;
+        const float v = k < MC ? __ldg(tcm + r * MC + k) : 0.f;
+        __nv_bfloat16 bh, bl;
+        tc::split_bf16(v, bh, bl);
+        h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
+        l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
+      }
+    }
+    const uint32_t off = tc::kmajor_offset(r, 8 * c, KP);
+    *reinterpret_cast<uint4*>(bop + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(bop + b_half + off) = make_uint4(l[0], l[1], l[2], l[3]);
   }
   tc::fence_proxy_async();
   tc::fence_before_sync();
@@ -135,7 +170,7 @@ __global__ void __launch_bounds__(NT, 1)
 #pragma unroll
     for (int mt = 0; mt < MT; ++mt) {
       const uint32_t d = taddr + (uint32_t)(mt * NP);
-      const uint32_t at = (uint32_t)mt * 16u * sbo;  // 16 row groups per tile
+      const uint32_t at = (uint32_t)(tile_row0(mt) / 8) * sbo;
 #pragma unroll 1
       for (int ks = 0; ks < KP / 16; ++ks) {
         const uint32_t step = (uint32_t)ks * 256u;
@@ -156,7 +191,7 @@ __global__ void __launch_bounds__(NT, 1)
     const int w = tid >> 5, lane = tid & 31;
     if (w < 4 * MT) {
       const int mt = w >> 2, sub = w & 3;
-      const int row = mt * 128 + sub * 32 + lane;
+      const int row = tile_row0(mt) + sub * 32 + lane;
 #pragma unroll
       for (int c0 = 0; c0 < NP; c0 += 32) {
         float v[32];
