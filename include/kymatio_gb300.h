@@ -170,6 +170,40 @@ int kym_s1d_backward(const kym_s1d_plan* plan, const float* x, const float* grad
                      const float* const* filters, int n_filters, void* workspace, size_t workspace_bytes,
                      void* stream);
 
+/* ------------------------------------------------------------------------
+ * Operator surface (float32, interleaved complex), for driving the reference
+ * frontend and core op by op.  batch counts the leading dimensions.
+ * ---------------------------------------------------------------------- */
+/* Batched 2-D DFT of M x N images (M = 1: 1-D lines of length N).  in_real:
+ * input is real (trailing dim 1); out_real: write the real part only; inverse:
+ * conjugate direction; every output is multiplied by scale.
+ * rfft = (in_real, !out_real, fwd, 1); ifft = (!in_real, !out_real, inv,
+ * 1/(MN)); irfft = (!in_real, out_real, inv, 1/(MN)).  Replaces
+ * TorchBackend2D.rfft/ifft/irfft (kymatio/scattering2d/backend/torch_backend.py:
+ * 131-155) and TorchBackend1D.rfft/ifft/irfft/cfft
+ * (kymatio/scattering1d/backend/torch_backend.py:108-141). */
+int kym_op_fft2(const float* in, float* out, int batch, int M, int N, int in_real, int out_real, int inverse,
+                float scale, void* stream);
+/* C[b, i] = A[b, i] * B[i] for i < n (B real, or complex when b_complex):
+ * TorchBackend.cdgmm (kymatio/backend/torch_backend.py:147-219). */
+int kym_op_cdgmm(const float* A, const float* B, float* C, long long batch, long long n, int b_complex, void* stream);
+/* |x| and its adjoint x g / |x| (0 where |x| = 0): ModulusStable
+ * (kymatio/backend/torch_backend.py:5-96). */
+int kym_op_modulus(const float* x, float* y, long long n, void* stream);
+int kym_op_modulus_backward(const float* x, const float* g, float* gx, long long n, void* stream);
+/* Periodisation (mean of kr x kc aliases) of complex (batch, M, N) and its
+ * adjoint (tiling / (kr kc)): subsample_fourier (kymatio/scattering2d/backend/
+ * torch_backend.py:92-129, kymatio/scattering1d/backend/torch_backend.py:18-48). */
+int kym_op_subsample(const float* x, float* y, int batch, int M, int N, int kr, int kc, void* stream);
+int kym_op_subsample_adjoint(const float* g, float* gx, int batch, int M, int N, int kr, int kc, void* stream);
+/* Reflect padding of real (batch, M, N) and its adjoint: Pad
+ * (kymatio/scattering2d/backend/torch_backend.py:19-86) and TorchBackend1D.pad
+ * (kymatio/scattering1d/backend/torch_backend.py:50-82). */
+int kym_op_reflect_pad(const float* x, float* y, int batch, int M, int N, int top, int bottom, int left, int right,
+                       void* stream);
+int kym_op_reflect_pad_adjoint(const float* g, float* gx, int batch, int M, int N, int top, int bottom, int left,
+                               int right, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,14 @@ SIGNATURES = {
     'kym_s1d_forward': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
     'kym_s1d_backward_workspace_bytes': (_c_size, [_vp, _c_int]),
     'kym_s1d_backward': (_c_int, [_vp, _vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
+    'kym_op_fft2': (_c_int, [_vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, ctypes.c_float, _vp]),
+    'kym_op_cdgmm': (_c_int, [_vp, _vp, _vp, ctypes.c_longlong, ctypes.c_longlong, _c_int, _vp]),
+    'kym_op_modulus': (_c_int, [_vp, _vp, ctypes.c_longlong, _vp]),
+    'kym_op_modulus_backward': (_c_int, [_vp, _vp, _vp, ctypes.c_longlong, _vp]),
+    'kym_op_subsample': (_c_int, [_vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
+    'kym_op_subsample_adjoint': (_c_int, [_vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
+    'kym_op_reflect_pad': (_c_int, [_vp, _vp] + [_c_int] * 7 + [_vp]),
+    'kym_op_reflect_pad_adjoint': (_c_int, [_vp, _vp] + [_c_int] * 7 + [_vp]),
 }
 
 _lock = threading.Lock()

@@ -112,3 +112,24 @@ def test_separable_lowpass_identity(M, J):
         ref = np.fft.ifft2(B).real[1:-1, 1:-1]
         got = Tr @ U @ Tc.T
         assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-6
+
+
+def test_reference_frontend_accepts_backend_objects():
+    """The reference frontends accept the GB300 backend objects (name check of
+    kymatio/frontend/base_frontend.py:47-50); runs when KYMATIO_REFERENCE
+    points at a reference checkout."""
+    import sys
+    ref = os.environ.get('KYMATIO_REFERENCE', '')
+    if not ref or not os.path.isdir(ref):
+        pytest.skip('KYMATIO_REFERENCE not set')
+    sys.path.insert(0, ref)
+    try:
+        from kymatio.scattering2d.frontend.torch_frontend import ScatteringTorch2D
+        from kymatio.scattering1d.frontend.torch_frontend import ScatteringTorch1D
+    finally:
+        sys.path.remove(ref)
+    from kymatio_gb300.backend import backend1d, backend2d
+    S2 = ScatteringTorch2D(2, (32, 32), backend=backend2d)
+    assert S2.backend is backend2d
+    S1 = ScatteringTorch1D(4, 256, backend=backend1d)
+    assert S1.backend is backend1d
