@@ -186,7 +186,8 @@ def test_op_level_cascade_1d_vs_oracle(dev):
             bank.append(d)
         banks.append(bank)
     U0 = B.pad(torch.from_numpy(x).to(dev).reshape(-1, 1, 1024), S.pad_left, S.pad_right)
-    paths = list(core.scattering1d(U0, B, [phi] + banks, S.log2_stride, True))
+    paths = sorted(core.scattering1d(U0, B, [phi] + banks, S.log2_stride, True),
+                   key=lambda p: (len(p['n']), p['n']))  # the frontend's ordering
     res = S.log2_stride
     out = torch.stack([B.unpad(p['coef'], S.ind_start[res], S.ind_end[res]) for p in paths], dim=-2)
     ref = Oracle(5, 1024, Q=4)(x.astype(np.float64))
