@@ -196,6 +196,83 @@ def order_rel_l2(out, ref):
     return res
 
 
+def _time_ms(fn, steps, warmup, flush):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        tot += e0.elapsed_time(e1)
+    return tot / steps
+
+
+def extras(dev, flush, steps=5, warmup=3):
+    """The other workloads: throughput at 32x32 J=2 (batch 128), 1-D N=8192
+    J=6 Q=(8,1) T=64 (batch 256), forward+backward / forward at 128x128 J=4
+    (batch 32), and the mixed 512-image batch of sides {32,64,128,256}."""
+    import torch
+    from kymatio_gb300 import Scattering2D
+    from kymatio_gb300.batching import MixedScattering2D, default_J
+    from kymatio_gb300.scattering1d import Scattering1D
+    res = {}
+    # 32x32, J=2, batch 128, U[0,1) seed 0
+    x = torch.from_numpy(np.random.default_rng(0).random((128, 32, 32)).astype(np.float32)).to(dev)
+    S = Scattering2D(2, (32, 32)).to(dev)
+    ms = _time_ms(lambda: S(x), steps, warmup, flush)
+    S.tensor_cores = True
+    ms_tc = _time_ms(lambda: S(x), steps, warmup, flush)
+    res['scattering2d_32x32_J2_b128'] = {'img_s': 128 / ms * 1e3, 'img_s_tc': 128 / ms_tc * 1e3}
+    # 1-D: white noise plus a linear chirp, seed 1
+    rng = np.random.default_rng(1)
+    N, B = 8192, 256
+    t = np.arange(N)
+    f0 = rng.uniform(0.01, 0.1, B)[:, None]
+    f1 = rng.uniform(0.1, 0.4, B)[:, None]
+    sig = rng.standard_normal((B, N)) + np.cos(2 * np.pi * (f0 * t + (f1 - f0) * t ** 2 / (2 * N)))
+    xs = torch.from_numpy(sig.astype(np.float32)).to(dev)
+    S1 = Scattering1D(6, N, Q=(8, 1), T=64).to(dev)
+    ms = _time_ms(lambda: S1(xs), steps, warmup, flush)
+    res['scattering1d_8192_J6_Q8_T64_b256'] = {'sig_s': B / ms * 1e3}
+    # 128x128, J=4, batch 32: forward vs forward + hand-written backward
+    rng = np.random.default_rng(3)
+    x4 = torch.from_numpy(rng.random((32, 128, 128)).astype(np.float32)).to(dev)
+    g4 = torch.from_numpy(rng.standard_normal((32, 417, 8, 8)).astype(np.float32)).to(dev)
+    S4 = Scattering2D(4, (128, 128)).to(dev)
+    fwd = _time_ms(lambda: S4(x4), steps, warmup, flush)
+    xr = x4.clone().requires_grad_()
+
+    def fb():
+        xr.grad = None
+        S4(xr).backward(g4)
+    fwdbwd = _time_ms(fb, steps, warmup, flush)
+    res['scattering2d_128x128_J4_b32_fwd_bwd'] = {'fwd_ms': fwd, 'fwd_bwd_ms': fwdbwd, 'ratio': fwdbwd / fwd}
+    # mixed batch: 512 images, sides drawn from {32,64,128,256}, seed 4
+    rng = np.random.default_rng(4)
+    sides = rng.choice([32, 64, 128, 256], size=512)
+    imgs = [torch.from_numpy(rng.random((s, s)).astype(np.float32)).to(dev) for s in sides]
+    groups = {}
+    for im in imgs:
+        groups.setdefault(int(im.shape[-1]), []).append(im)
+    xs = {s: torch.stack(v) for s, v in groups.items()}
+    mods = {s: Scattering2D(default_J(s), (s, s)).to(dev) for s in xs}
+    seq = _time_ms(lambda: [mods[s](xs[s]) for s in sorted(xs)], steps, warmup, flush)
+    mix = MixedScattering2D(list(xs)).to(dev)
+    gr = _time_ms(lambda: mix.forward_grouped(xs), steps, warmup, flush)
+    mixt = MixedScattering2D(list(xs), tensor_cores=True).to(dev)
+    grt = _time_ms(lambda: mixt.forward_grouped(xs), steps, warmup, flush)
+    res['mixed_512_sides_32_64_128_256'] = {
+        'img_s_per_size_sequential': 512 / seq * 1e3, 'img_s_graph': 512 / gr * 1e3,
+        'img_s_graph_tc': 512 / grt * 1e3, 'counts': {str(s): len(v) for s, v in sorted(groups.items())}}
+    return res
+
+
 def run_ours(args, world, rank, local):
     import ctypes
     import torch
@@ -342,6 +419,9 @@ def run_ours(args, world, rank, local):
         cpu = {'value': rate, 'unit': 'img/s', 'cores': threads, 'kind': 'port',
                'sample': '8 GRF images (%.1f s), oracle port of the reference numpy backend in fp32, '
                          'scipy.fft workers=%d' % (sec, threads)}
+    extra = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        extra = extras(dev, flush)
     if rank == 0:
         line = {
             'metric': METRIC, 'value': value, 'unit': 'img/s', 'n_gpus': world, 'steps': args.steps,
@@ -371,6 +451,7 @@ def run_ours(args, world, rank, local):
             'group_ms_per_step': [round(v, 4) for v in g_tc],
             'clocks': clocks,
             'cpu_baseline': cpu,
+            'extras': extra,
         }
         print(json.dumps(line), flush=True)
 
@@ -383,6 +464,7 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--chunk', type=int, default=0)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-extras', action='store_true', help='skip the other workloads')
     ap.add_argument('--batch', type=int, default=64, help='images per GPU (64 is the benchmark workload)')
     args = ap.parse_args()
     global BATCH

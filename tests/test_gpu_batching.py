@@ -1,0 +1,49 @@
+"""Mixed-size batches (kymatio_gb300.batching): one CUDA graph over size
+groups on separate streams gives the same coefficients as per-size modules."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+torch = pytest.importorskip('torch')
+pytestmark = pytest.mark.gpu
+
+
+def test_mixed_batch_graph_matches_per_size(tmp_path, monkeypatch):
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    monkeypatch.setenv('KYMATIO_GB300_CACHE', str(tmp_path))
+    from kymatio_gb300 import Scattering2D
+    from kymatio_gb300.batching import MixedScattering2D, default_J
+    dev = torch.device('cuda:0')
+    rng = np.random.default_rng(4)
+    sides = rng.choice([32, 64, 128, 256], size=24)
+    imgs = [torch.from_numpy(rng.random((s, s)).astype(np.float32)).to(dev) for s in sides]
+    M = MixedScattering2D([32, 64, 128, 256], graph=True, tune=True).to(dev)
+    for rep in range(2):  # capture, then replay with new data
+        if rep:
+            imgs = [torch.rand_like(im) for im in imgs]
+        out = M(imgs)
+        torch.cuda.synchronize()
+        for im, o in zip(imgs, out):
+            s = im.shape[-1]
+            ref = Scattering2D(default_J(s), (s, s)).to(dev)(im[None])[0]
+            assert o.shape == ref.shape
+            assert rel_l2(o.cpu().numpy(), ref.cpu().numpy()) <= 1e-6
+    assert (tmp_path / 'autotune.json').exists()
+
+
+def test_mixed_batch_tensor_cores():
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from kymatio_gb300.batching import MixedScattering2D, default_J
+    from oracle.scattering2d import Scattering2D as Oracle
+    dev = torch.device('cuda:0')
+    rng = np.random.default_rng(5)
+    imgs = [torch.from_numpy(rng.random((s, s)).astype(np.float32)).to(dev) for s in (32, 64, 128, 64)]
+    M = MixedScattering2D([32, 64, 128], tensor_cores=True).to(dev)
+    out = M(imgs)
+    for im, o in zip(imgs, out):
+        s = im.shape[-1]
+        ref = Oracle(default_J(s), (s, s))(im.cpu().numpy()[None].astype(np.float64))[0]
+        assert rel_l2(o.cpu().numpy(), ref) <= 5e-5
