@@ -63,6 +63,27 @@ __global__ void reflect_pad_adjoint_kernel(const float* __restrict__ gpad, long 
   gx[(size_t)(img0 + img) * M * N + rem] = acc;
 }
 
+__global__ void bwd_gather_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather,
+                                  FilterTable F, int mr, int mc, float2* __restrict__ gy, long long gy_stride,
+                                  const float2* __restrict__ gyc, long long gyc_stride) {
+  const BwdTask t = tasks[blockIdx.y];
+  if (t.gather_count == 0) return;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= mr * mc) return;
+  const int u = e / mc, v = e - (e / mc) * mc;
+  const size_t img = blockIdx.z;
+  const float2* yc = gyc + img * gyc_stride;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int c = 0; c < t.gather_count; ++c) {
+    const GatherItem gi = gather[t.gather_first + c];
+    const float w = __ldg(F.f[gi.psi] + e) / (float)(gi.kr * gi.kc);
+    const float2 y = __ldg(yc + gi.gy_off + (size_t)(u % gi.mr) * gi.mc + (v % gi.mc));
+    acc.x = fmaf(y.x, w, acc.x);
+    acc.y = fmaf(y.y, w, acc.y);
+  }
+  gy[img * gy_stride + t.gy_off + e] = acc;
+}
+
 namespace {
 struct BwdEntry {
   int mr, mc, sr, sc, c;

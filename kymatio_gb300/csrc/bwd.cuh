@@ -201,23 +201,24 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
 
   // 2. g_U^ = phi * tile(g_B) / ks^2 + sum_c psi_c * tile(g_Y_c) / k_c^2
   const float* phi = F.f[t.phi];
-  const float2* gyc = L.gyc ? L.gyc + (size_t)img * L.gyc_stride : nullptr;
   const int nloc = RL * MC;
   for (int i = threadIdx.x; i < nloc; i += NT) {
     const int u = i / MC, v = i % MC;
     const int gu = row0 + u;
-    const size_t gidx = (size_t)gu * MC + v;
-    const float f = __ldg(phi + gidx) * L.gb_scale;
+    const float f = __ldg(phi + (size_t)gu * MC + v) * L.gb_scale;
     const float2 b = *bat(gu % SR, v % SC);
-    float2 acc = make_float2(b.x * f, b.y * f);
-    for (int c = 0; c < t.gather_count; ++c) {
-      const GatherItem gi = L.gather[t.gather_first + c];
-      const float w = __ldg(F.f[gi.psi] + gidx) / (float)(gi.kr * gi.kc);
-      const float2 y = __ldg(gyc + gi.gy_off + (size_t)(gu % gi.mr) * gi.mc + (v % gi.mc));
-      acc.x = fmaf(y.x, w, acc.x);
-      acc.y = fmaf(y.y, w, acc.y);
+    *at(u, v) = make_float2(b.x * f, b.y * f);
+  }
+  // children's contributions, summed beforehand by bwd_gather_kernel into
+  // this task's gradient block (complex, full m x m)
+  if (t.gather_count > 0) {
+    const float2* pre = L.gy + (size_t)img * L.gy_stride + t.gy_off + (size_t)row0 * MC;
+    for (int i = threadIdx.x; i < nloc; i += NT) {
+      const float2 y = __ldg(pre + i);
+      float2* p = at(i / MC, i % MC);
+      p->x += y.x;
+      p->y += y.y;
     }
-    *at(u, v) = acc;
   }
   __syncthreads();
 
@@ -298,6 +299,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   const RtEngine<CL, ONED> e{L, A, B, rank, rowp};
   bwd_body(e, L, F);
 }
+
+// Children's contributions to a parent's spectrum gradient:
+//   out[img][task][u][v] = sum_c psi_c[u][v] * g_Y_c[u mod mr_c][v mod mc_c] / (kr_c kc_c)
+// written into each task's gradient block (complex, mr x mc).  One thread
+// per element; grid = (element blocks, tasks, images).
+__global__ void bwd_gather_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather,
+                                  FilterTable F, int mr, int mc, float2* __restrict__ gy, long long gy_stride,
+                                  const float2* __restrict__ gyc, long long gyc_stride);
 
 // Reflect-pad adjoint: g_x[i][j] = sum of g_pad over the padded positions that
 // reflect onto (i, j) (kymatio/scattering2d/backend/torch_backend.py:56-57,

@@ -471,7 +471,10 @@ static int make_filter_table(CascadePlan* P, const float* const* filters, int nf
 static int run_core(CascadePlan* P, const float* x, float* out, int batch, const FilterTable& F, const RunArgs& a,
                     cudaStream_t stream) {
   const DeviceState* ds = a.ds;
-  const int chunk = std::max(1, std::min(batch, a.chunk));
+  // equal chunks: ceil(batch / n) images each for the fewest chunks n
+  int chunk = std::max(1, std::min(batch, a.chunk));
+  const int nch = (batch + chunk - 1) / chunk;
+  chunk = (batch + nch - 1) / nch;
   const long long x_stride = (long long)P->img_M * P->img_N;
   const long long out_stride = (long long)P->channels * P->out_nr * P->out_nc;
   cudaError_t err = cudaSuccess;
@@ -820,7 +823,9 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
   }
   const DeviceState* ds = device_state(P);
   if (!ds) return fail_cuda(cudaGetLastError(), "plan table upload");
-  const int chunk = std::min(batch, P->bchunk);
+  int chunk = std::min(batch, P->bchunk);
+  const int nch = (batch + chunk - 1) / chunk;
+  chunk = (batch + nch - 1) / nch;
   float2* u0 = static_cast<float2*>(workspace);
   float2* u1 = u0 + (size_t)chunk * P->u0_elems;
   float2* gy2 = u1 + (size_t)chunk * P->u1_elems;
@@ -923,6 +928,16 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
         L.gy_stride = P->u0_elems;
         L.gyc = gy1;
         L.gyc_stride = P->gy1_elems;
+      }
+      bool any_gather = false;
+      for (const BwdTask& bt : b.tasks) any_gather |= bt.gather_count > 0;
+      if (any_gather) {
+        const int elems = L.mr * L.mc;
+        dim3 grid((elems + 255) / 256, L.ntasks, nimg);
+        bwd_gather_kernel<<<grid, 256, 0, stream>>>(L.tasks, L.gather, F, L.mr, L.mc, L.gy, L.gy_stride, L.gyc,
+                                                      L.gyc_stride);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return fail_cuda(err, "backward gather");
       }
       if (b.has_ct) err = b.ct(L, F, nimg, stream);
       else if (g.oned) err = launch_rt_bwd<false, true>(b, L, F, nimg, stream);
