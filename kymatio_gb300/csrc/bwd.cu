@@ -63,25 +63,58 @@ __global__ void reflect_pad_adjoint_kernel(const float* __restrict__ gpad, long 
   gx[(size_t)(img0 + img) * M * N + rem] = acc;
 }
 
+// One block per (strip of kGatherRows rows x tile of blockDim columns, task,
+// image); one thread per column.  The task's gather list is staged in shared memory
+// kGatherMax items at a time; per child the column residue is one division
+// and the row residue advances incrementally.
+constexpr int kGatherRows = 8;
+constexpr int kGatherMax = 64;
+
 __global__ void bwd_gather_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather,
                                   FilterTable F, int mr, int mc, float2* __restrict__ gy, long long gy_stride,
                                   const float2* __restrict__ gyc, long long gyc_stride) {
+  __shared__ GatherItem items[kGatherMax];
   const BwdTask t = tasks[blockIdx.y];
   if (t.gather_count == 0) return;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= mr * mc) return;
-  const int u = e / mc, v = e - (e / mc) * mc;
   const size_t img = blockIdx.z;
   const float2* yc = gyc + img * gyc_stride;
-  float2 acc = make_float2(0.f, 0.f);
-  for (int c = 0; c < t.gather_count; ++c) {
-    const GatherItem gi = gather[t.gather_first + c];
-    const float w = __ldg(F.f[gi.psi] + e) / (float)(gi.kr * gi.kc);
-    const float2 y = __ldg(yc + gi.gy_off + (size_t)(u % gi.mr) * gi.mc + (v % gi.mc));
-    acc.x = fmaf(y.x, w, acc.x);
-    acc.y = fmaf(y.y, w, acc.y);
+  float2* out = gy + img * gy_stride + t.gy_off;
+  // blockIdx.x = strip * column tiles + tile (long 1-D rows span several tiles)
+  const int ctiles = (mc + blockDim.x - 1) / blockDim.x;
+  const int u0 = (blockIdx.x / ctiles) * kGatherRows;
+  const int u1 = min(u0 + kGatherRows, mr);
+  const int v = (blockIdx.x % ctiles) * blockDim.x + threadIdx.x;
+  float2 acc[kGatherRows];
+#pragma unroll
+  for (int r = 0; r < kGatherRows; ++r) acc[r] = make_float2(0.f, 0.f);
+  for (int c0 = 0; c0 < t.gather_count; c0 += kGatherMax) {
+    const int nc = min(t.gather_count - c0, kGatherMax);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) items[i] = gather[t.gather_first + c0 + i];
+    __syncthreads();
+    if (v >= mc) continue;
+    for (int c = 0; c < nc; ++c) {
+      const GatherItem gi = items[c];
+      const float* psi = F.f[gi.psi];
+      const float w = 1.f / (float)(gi.kr * gi.kc);
+      const float2* ycol = yc + gi.gy_off + (v % gi.mc);
+      int um = u0 % gi.mr;
+#pragma unroll
+      for (int r = 0; r < kGatherRows; ++r) {
+        if (u0 + r < u1) {
+          const float f = __ldg(psi + (size_t)(u0 + r) * mc + v) * w;
+          const float2 y = __ldg(ycol + (size_t)um * gi.mc);
+          acc[r].x = fmaf(y.x, f, acc[r].x);
+          acc[r].y = fmaf(y.y, f, acc[r].y);
+        }
+        if (++um == gi.mr) um = 0;
+      }
+    }
   }
-  gy[img * gy_stride + t.gy_off + e] = acc;
+  if (v < mc)
+#pragma unroll
+    for (int r = 0; r < kGatherRows; ++r)
+      if (u0 + r < u1) out[(size_t)(u0 + r) * mc + v] = acc[r];
 }
 
 namespace {

@@ -932,9 +932,10 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
       bool any_gather = false;
       for (const BwdTask& bt : b.tasks) any_gather |= bt.gather_count > 0;
       if (any_gather) {
-        const int elems = L.mr * L.mc;
-        dim3 grid((elems + 255) / 256, L.ntasks, nimg);
-        bwd_gather_kernel<<<grid, 256, 0, stream>>>(L.tasks, L.gather, F, L.mr, L.mc, L.gy, L.gy_stride, L.gyc,
+        const int threads = std::min(512, (L.mc + 31) / 32 * 32);  // one thread per column
+        const int ctiles = (L.mc + threads - 1) / threads;
+        dim3 grid((L.mr + 7) / 8 * ctiles, L.ntasks, nimg);
+        bwd_gather_kernel<<<grid, threads, 0, stream>>>(L.tasks, L.gather, F, L.mr, L.mc, L.gy, L.gy_stride, L.gyc,
                                                       L.gyc_stride);
         err = cudaGetLastError();
         if (err != cudaSuccess) return fail_cuda(err, "backward gather");
