@@ -17,6 +17,7 @@
 // kernel).  The modulus phase y is recomputed from the parent spectrum.
 #pragma once
 #include "cascade.cuh"
+#include "ct_cascade.cuh"
 #include "ct_engine.cuh"
 
 namespace kym {
@@ -60,6 +61,7 @@ struct BwdLaunch {
   int ntasks;
   const GatherItem* gather;
   int img0;
+  const float2* tw_rl;  // local column length of a cluster split (mr / cluster)
 };
 
 // ---------------------------------------------------------------------------
@@ -84,17 +86,16 @@ struct CtEngine {
   __device__ int ld() const { return LD; }
   __device__ int ldb() const { return LDB; }
   __device__ int rl() const { return RL; }
-  __device__ __forceinline__ void fft2(bool inv) const {
+  static constexpr bool kPerm = (C > 1);  // dif leaves rows permuted across the cluster
+  // natural rows in; a cluster leaves row k1 + C k2 at CTA k1, local row k2
+  __device__ __forceinline__ void fft2_dif(bool inv) const {
     ct::fft_lines<MC, RL, NT>(ct::RowLines<LD, ONED>{A}, 0, L.prow.tw, inv);
-    if constexpr (!ONED) {
-      if constexpr (C > 1) {
-        ct::cluster_sync();
-        ct::fft_lines<MR, MC / C, NT>(ct::ClusterColLines<LD, RL>{ct::smem_u32(A)}, rank * (MC / C), L.pcol.tw,
-                                      inv);
-      } else {
-        ct::fft_lines<MR, MC, NT>(ct::ColLines<LD>{A}, 0, L.pcol.tw, inv);
-      }
-    }
+    if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, inv, true);
+  }
+  // that permuted layout in, natural rows out
+  __device__ __forceinline__ void fft2_dit(bool inv) const {
+    if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, inv, false);
+    ct::fft_lines<MC, RL, NT>(ct::RowLines<LD, ONED>{A}, 0, L.prow.tw, inv);
   }
   __device__ __forceinline__ void small_fft2(bool inv) const {
     ct::fft_lines<SC, SR, NT>(ct::RowLines<LDB, ONED>{B}, 0, L.psrow.tw, inv);
@@ -135,6 +136,7 @@ struct RtEngine {
     w.rank = rank;
     return w;
   }
+  static constexpr bool kPerm = false;  // runtime plans keep natural rows
   __device__ void fft2(bool inv) const {
     const Slab w = slab();
     fft_pass<true, ONED, false>(w, L.rows_local, 0, L.prow, inv, Barrier{false});
@@ -144,6 +146,8 @@ struct RtEngine {
       fft_pass<false, false, CL>(w, cpc, rank * cpc, L.pcol, inv, Barrier{CL});
     }
   }
+  __device__ void fft2_dif(bool inv) const { fft2(inv); }
+  __device__ void fft2_dit(bool inv) const { fft2(inv); }
   __device__ void small_fft2(bool inv) const {
     Slab w;
     w.local = B;
@@ -223,10 +227,20 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
   __syncthreads();
 
   // 3. g_U = Re IFFT2u(g_U^)
-  e.fft2(true);
-  float* gu_out = reinterpret_cast<float*>(L.gy + (size_t)img * L.gy_stride + t.gy_off) + (size_t)row0 * MC;
+  e.fft2_dif(true);
+  float* gu_base = reinterpret_cast<float*>(L.gy + (size_t)img * L.gy_stride + t.gy_off);
+  float* gu_out = gu_base + (size_t)row0 * MC;
+  if (L.level == 0) {
+    // g_pad in natural rows for the reflect-pad adjoint
+    for (int i = threadIdx.x; i < nloc; i += NT) {
+      const int u = i / MC, v = i % MC;
+      const int grow = E::kPerm ? e.rank + L.cluster * u : row0 + u;
+      gu_base[(size_t)grow * MC + v] = at(u, v)->x;
+    }
+    return;
+  }
+  // levels 1 and 2 keep g_U in this CTA's (possibly permuted) rows
   for (int i = threadIdx.x; i < nloc; i += NT) gu_out[i] = at(i / MC, i % MC)->x;
-  if (L.level == 0) return;  // g_pad done; the reflect-pad adjoint runs next
 
   // 4. recompute y = IFFT2(fold(P * psi)) for the modulus phase
   __syncthreads();  // g_U stores visible to this CTA before they are re-read in step 5
@@ -249,7 +263,7 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
     *at(u, v) = cscale(acc, L.rec_scale);
   }
   __syncthreads();
-  e.fft2(true);
+  e.fft2_dif(true);
 
   // 5. g_y = g_U * y / |y|  (zero where |y| == 0)
   for (int i = threadIdx.x; i < nloc; i += NT) {
@@ -262,7 +276,7 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
   __syncthreads();
 
   // 6. g_Y = FFT2(g_y) / m^2, written over g_U (already consumed)
-  e.fft2(false);
+  e.fft2_dit(false);
   float2* gy_out = L.gy + (size_t)img * L.gy_stride + t.gy_off + (size_t)row0 * MC;
   for (int i = threadIdx.x; i < nloc; i += NT) gy_out[i] = cscale(*at(i / MC, i % MC), L.gy_scale);
 }

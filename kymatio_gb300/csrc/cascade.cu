@@ -383,6 +383,7 @@ static int make_group(CascadePlan* P, Group& g, int mr, int mc, int kr, int kc, 
     if (!C) return KYM_ERR_UNSUPPORTED;
     L.cluster = C;
     L.rows_local = mr / C;
+    if (C > 1) P->tw.add(mr / C);
   }
   static_assert(sizeof(int) == 4, "");
   if (g_use_ct) {
@@ -495,6 +496,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
       L.pcol.tw = ds->tw + P->tw.offset(L.pcol.n);
       L.psrow.tw = ds->tw + P->tw.offset(L.psrow.n);
       L.pscol.tw = ds->tw + P->tw.offset(L.pscol.n);
+      L.tw_rl = L.cluster > 1 ? ds->tw + P->tw.offset(L.mr / L.cluster) : nullptr;
       L.x = x;
       L.x_stride = x_stride;
       L.out = out;
@@ -854,6 +856,7 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
       L.pcol.tw = ds->tw + P->tw.offset(L.pcol.n);
       L.psrow.tw = ds->tw + P->tw.offset(L.psrow.n);
       L.pscol.tw = ds->tw + P->tw.offset(L.pscol.n);
+      L.tw_rl = L.cluster > 1 ? ds->tw + P->tw.offset(L.mr / L.cluster) : nullptr;
       L.x = x;
       L.x_stride = (long long)P->img_M * P->img_N;
       L.img0 = c0;
@@ -896,6 +899,7 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
       L.pcol.tw = ds->tw + P->tw.offset(L.pcol.n);
       L.psrow.tw = ds->tw + P->tw.offset(L.psrow.n);
       L.pscol.tw = ds->tw + P->tw.offset(L.pscol.n);
+      L.tw_rl = L.cluster > 1 ? ds->tw + P->tw.offset(L.mr / L.cluster) : nullptr;
       L.level = b.level;
       L.out_r0 = g.L.out_r0;
       L.out_c0 = g.L.out_c0;

@@ -58,6 +58,7 @@ struct CascadeLaunch {
   int ntasks;
   int img0;     // first image of this chunk (for x/out offsets)
   int skip_s;   // 1: stop after storing the spectrum (backward recomputation)
+  const float2* tw_rl;  // exp(-2 pi i k / (mr / cluster)): local column length of a cluster split
 };
 
 }  // namespace kym

@@ -58,7 +58,10 @@ __device__ __forceinline__ void ct_load(float2* A, const CascadeLaunch& L, const
     const float* x = L.x + (size_t)(L.img0 + img) * L.x_stride;
     for (int e = threadIdx.x; e < NLOC; e += NT) {
       const int u = e / MC, v = e % MC;
-      const int iy = ONED ? 0 : ct_reflect(row0 + u - L.pad_t, L.img_M);
+      // clusters take the image rows permuted (CTA c, local row u = row c + C u),
+      // the layout the split column transform consumes
+      const int grow = C > 1 ? row0 / RL + C * u : row0 + u;
+      const int iy = ONED ? 0 : ct_reflect(grow - L.pad_t, L.img_M);
       const int ix = ct_reflect(v - L.pad_l, L.img_N);
       *at(u, v) = make_float2(__ldg(x + (size_t)iy * L.img_N + ix) * L.load_scale, 0.f);
     }
@@ -115,6 +118,78 @@ __device__ __forceinline__ void ct_load(float2* A, const CascadeLaunch& L, const
   }
 }
 
+// Cluster column transforms split as MR = C x RL (C CTAs, RL local rows).
+// DIF (natural rows in, CTA c holds rows RL c + n'):
+//   X[k1 + C k2] = sum_n' W_RL^{n' k2} [ W_MR^{n' k1} sum_c x[RL c + n'] W_C^{c k1} ]
+//   -> cross-CTA radix-C step (CTA k1 forms the bracket), then a local
+//      RL-point FFT; CTA k1 ends with rows k1 + C k2 at local row k2.
+// DIT (that permuted layout in):
+//   X[k2 + RL k1] = sum_c W_C^{c k1} W_MR^{c k2} sum_g W_RL^{g k2} x[c + C g]
+//   -> local RL-point FFT, then the cross-CTA step; CTA k1 ends with the
+//      natural rows RL k1 + k2.
+// Every remote element is read once; the in-place cross step runs in
+// rounds with a cluster barrier between a round's reads and its writes.
+template <int MR, int MC, int C, int LD, int NT, bool DIT>
+__device__ __forceinline__ void ct_cross(float2* A, int rank, const float2* __restrict__ tw, bool inv) {
+  constexpr int RL = MR / C;
+  constexpr int NEL = RL * MC;
+  constexpr int PER = 8;
+  constexpr int ROUNDS = (NEL + NT * PER - 1) / (NT * PER);
+  const uint32_t base = ct::smem_u32(A);
+  float2 wc[C];  // W_C^{c rank}
+#pragma unroll
+  for (int c = 0; c < C; ++c) wc[c] = conj_if(__ldg(tw + ((c * rank) % C) * RL), inv);
+#pragma unroll 1
+  for (int rd = 0; rd < ROUNDS; ++rd) {
+    float2 acc[PER];
+#pragma unroll
+    for (int it = 0; it < PER; ++it) {
+      const int e = threadIdx.x + (rd * PER + it) * NT;
+      acc[it] = make_float2(0.f, 0.f);
+      if (e < NEL) {
+        const int n = e / MC, col = e % MC;
+        const uint32_t off = base + (uint32_t)((n * LD + col) * 8);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const float2 x = (c == rank) ? A[n * LD + col] : ct::ld_dsmem(ct::mapa(off, (uint32_t)c));
+          float2 w = wc[c];
+          if (DIT) w = cmul(w, conj_if(__ldg(tw + (c * n) % MR), inv));
+          acc[it] = cadd(acc[it], cmul(x, w));
+        }
+        if (!DIT) acc[it] = cmul(acc[it], conj_if(__ldg(tw + (n * rank) % MR), inv));
+      }
+    }
+    ct::cluster_sync();  // every CTA has read this round's elements
+#pragma unroll
+    for (int it = 0; it < PER; ++it) {
+      const int e = threadIdx.x + (rd * PER + it) * NT;
+      if (e < NEL) A[(e / MC) * LD + (e % MC)] = acc[it];
+    }
+  }
+  __syncthreads();
+}
+
+// Column pass of the work array: local (C == 1) or split over the cluster.
+// dif: natural rows in, permuted out (C > 1); !dif: permuted in, natural out.
+template <int MR, int MC, int C, int LD, int NT>
+__device__ __forceinline__ void ct_cols(float2* A, int rank, const float2* tw, const float2* tw_rl, bool inv,
+                                        bool dif) {
+  if constexpr (C == 1) {
+    ct::fft_lines<MR, MC, NT>(ct::ColLines<LD>{A}, 0, tw, inv);
+  } else {
+    constexpr int RL = MR / C;
+    ct::cluster_sync();  // rows of every CTA complete
+    if (dif) {
+      ct_cross<MR, MC, C, LD, NT, false>(A, rank, tw, inv);
+      ct::fft_lines<RL, MC, NT>(ct::ColLines<LD>{A}, 0, tw_rl, inv);
+    } else {
+      ct::fft_lines<RL, MC, NT>(ct::ColLines<LD>{A}, 0, tw_rl, inv);
+      ct::cluster_sync();
+      ct_cross<MR, MC, C, LD, NT, true>(A, rank, tw, inv);
+    }
+  }
+}
+
 template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
 __global__ void __launch_bounds__(NT, 1)
     ct_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
@@ -141,48 +216,21 @@ __global__ void __launch_bounds__(NT, 1)
 
   const ct::RowLines<LD, ONED> rows{A};
   if (KF != 0 && L.modulus) {
+    // U = |IFFT2(A)| ; A = FFT2(U)  (a cluster leaves U in permuted rows)
     ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, true);
-    if constexpr (!ONED) {
-      if constexpr (C > 1) {
-        ct::cluster_sync();
-        const ct::ClusterColLines<LD, RL> cols{ct::smem_u32(A)};
-        ct::fft_lines<MR, MC / C, NT>(cols, rank * (MC / C), L.pcol.tw, true);
-      } else {
-        const ct::ColLines<LD> cols{A};
-        ct::fft_lines<MR, MC, NT>(cols, 0, L.pcol.tw, true);
-      }
-    }
+    if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, true, true);
     for (int e = threadIdx.x; e < NLOC; e += NT) {
       float2* p = at(e / MC, e % MC);
       const float2 z = *p;
       *p = make_float2(sqrtf(fmaf(z.x, z.x, z.y * z.y)), 0.f);
     }
-    if constexpr (!ONED) {
-      if constexpr (C > 1) {
-        ct::cluster_sync();
-        const ct::ClusterColLines<LD, RL> cols{ct::smem_u32(A)};
-        ct::fft_lines<MR, MC / C, NT>(cols, rank * (MC / C), L.pcol.tw, false);
-      } else {
-        __syncthreads();
-        const ct::ColLines<LD> cols{A};
-        ct::fft_lines<MR, MC, NT>(cols, 0, L.pcol.tw, false);
-      }
-    } else {
-      __syncthreads();
-    }
+    __syncthreads();
+    if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, false, false);
     ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, false);
   } else {
+    // the input stage: natural rows for one CTA, permuted rows for a cluster
     ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, false);
-    if constexpr (!ONED) {
-      if constexpr (C > 1) {
-        ct::cluster_sync();
-        const ct::ClusterColLines<LD, RL> cols{ct::smem_u32(A)};
-        ct::fft_lines<MR, MC / C, NT>(cols, rank * (MC / C), L.pcol.tw, false);
-      } else {
-        const ct::ColLines<LD> cols{A};
-        ct::fft_lines<MR, MC, NT>(cols, 0, L.pcol.tw, false);
-      }
-    }
+    if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, false, false);
   }
 
   // ---- parent spectrum for the next order --------------------------------------

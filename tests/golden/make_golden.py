@@ -122,6 +122,7 @@ GRAD_2D = [
     ('g2_j3_64x48', 3, (64, 48), 2, False, 1),
     ('g2_j1_31_prepad', 1, (31, 31), 2, True, 2),
     ('g2_j3_40_order1', 3, (40, 40), 1, False, 2),
+    ('g2_j3_256', 3, (256, 256), 2, False, 1),
 ]
 GRAD_1D = [
     ('g1_j5_q4_n1024', dict(J=5, shape=1024, Q=4), 2),
