@@ -252,7 +252,12 @@ def extras(dev, flush, steps=5, warmup=3):
         xr.grad = None
         S4(xr).backward(g4)
     fwdbwd = _time_ms(fb, steps, warmup, flush)
-    res['scattering2d_128x128_J4_b32_fwd_bwd'] = {'fwd_ms': fwd, 'fwd_bwd_ms': fwdbwd, 'ratio': fwdbwd / fwd}
+    S4.activation_budget = 0  # recompute form: only x kept, spectra and y recomputed
+    fwdbwd_rc = _time_ms(fb, steps, warmup, flush)
+    res['scattering2d_128x128_J4_b32_fwd_bwd'] = {
+        'fwd_ms': fwd, 'fwd_bwd_ms': fwdbwd, 'ratio': fwdbwd / fwd,
+        'policy': 'saved modulus inputs, %.1f MB (4 GiB budget)' % (S4._saved_bytes(32) / 1e6),
+        'fwd_bwd_ms_recompute': fwdbwd_rc, 'ratio_recompute': fwdbwd_rc / fwd}
     # mixed batch: 512 images, sides drawn from {32,64,128,256}, seed 4
     rng = np.random.default_rng(4)
     sides = rng.choice([32, 64, 128, 256], size=512)

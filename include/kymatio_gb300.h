@@ -107,11 +107,29 @@ int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);
  * into the workspace (kym_s2d_backward_workspace_bytes). */
 size_t kym_s2d_backward_workspace_bytes(const kym_s2d_plan* plan, int batch);
 /* Images per backward pass (bounds its workspace: the recomputed input and
- * parent spectra and the per-path gradient blocks of one chunk). */
+ * parent spectra and the per-path gradient blocks of one chunk; by default
+ * as many images as fit 1 GiB). */
 int kym_s2d_set_backward_chunk(kym_s2d_plan* plan, int chunk);
 int kym_s2d_backward(const kym_s2d_plan* plan, const float* x, const float* grad_out, float* grad_x, int batch,
                      const float* const* filters, int n_filters, void* workspace, size_t workspace_bytes,
                      void* stream);
+
+/* Saved-activation form of the forward/backward pair (what torch autograd
+ * does with the reference's op graph: the forward keeps what the backward
+ * needs, kymatio/backend/torch_backend.py:85-96 saves the modulus input).
+ * kym_s2d_forward_save computes exactly kym_s2d_forward's output and also
+ * stores every order-1 and order-2 path's modulus input y = IFFT2(...)
+ * (complex64) into `saved` (kym_s2d_saved_bytes(plan, batch) bytes);
+ * kym_s2d_backward_saved then needs neither x nor any recomputation.  The
+ * frontend picks this form while batch x saved bytes per image stays under
+ * its activation budget, and the recomputing kym_s2d_backward above it. */
+size_t kym_s2d_saved_bytes(const kym_s2d_plan* plan, int batch);
+int kym_s2d_forward_save(const kym_s2d_plan* plan, const float* x, float* out, int batch,
+                         const float* const* filters, int n_filters, void* workspace, size_t workspace_bytes,
+                         void* saved, size_t saved_bytes, void* stream);
+int kym_s2d_backward_saved(const kym_s2d_plan* plan, const void* saved, size_t saved_bytes, const float* grad_out,
+                           float* grad_x, int batch, const float* const* filters, int n_filters, void* workspace,
+                           size_t workspace_bytes, void* stream);
 
 /* Allocation-free forward.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (a fixed memory pool reserved up
@@ -169,6 +187,14 @@ size_t kym_s1d_backward_workspace_bytes(const kym_s1d_plan* plan, int batch);
 int kym_s1d_backward(const kym_s1d_plan* plan, const float* x, const float* grad_out, float* grad_x, int batch,
                      const float* const* filters, int n_filters, void* workspace, size_t workspace_bytes,
                      void* stream);
+/* Saved-activation form, as kym_s2d_saved_bytes / _forward_save / _backward_saved. */
+size_t kym_s1d_saved_bytes(const kym_s1d_plan* plan, int batch);
+int kym_s1d_forward_save(const kym_s1d_plan* plan, const float* x, float* out, int batch,
+                         const float* const* filters, int n_filters, void* workspace, size_t workspace_bytes,
+                         void* saved, size_t saved_bytes, void* stream);
+int kym_s1d_backward_saved(const kym_s1d_plan* plan, const void* saved, size_t saved_bytes, const float* grad_out,
+                           float* grad_x, int batch, const float* const* filters, int n_filters, void* workspace,
+                           size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------------------
  * Operator surface (float32, interleaved complex), for driving the reference

@@ -39,6 +39,11 @@ SIGNATURES = {
     'kym_s2d_backward_workspace_bytes': (_c_size, [_vp, _c_int]),
     'kym_s2d_set_backward_chunk': (_c_int, [_vp, _c_int]),
     'kym_s2d_backward': (_c_int, [_vp, _vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
+    'kym_s2d_saved_bytes': (_c_size, [_vp, _c_int]),
+    'kym_s2d_forward_save': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp, _c_size,
+                                      _vp]),
+    'kym_s2d_backward_saved': (_c_int, [_vp, _vp, _c_size, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp,
+                                        _c_size, _vp]),
     'kym_s2d_forward_tc': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, ctypes.POINTER(_vp),
                                     ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp, _vp,
                                     ctypes.POINTER(ctypes.c_float), _c_int]),
@@ -57,6 +62,11 @@ SIGNATURES = {
     'kym_s1d_forward': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
     'kym_s1d_backward_workspace_bytes': (_c_size, [_vp, _c_int]),
     'kym_s1d_backward': (_c_int, [_vp, _vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp]),
+    'kym_s1d_saved_bytes': (_c_size, [_vp, _c_int]),
+    'kym_s1d_forward_save': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp, _c_size,
+                                      _vp]),
+    'kym_s1d_backward_saved': (_c_int, [_vp, _vp, _c_size, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, _vp,
+                                        _c_size, _vp]),
     'kym_op_fft2': (_c_int, [_vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, ctypes.c_float, _vp]),
     'kym_op_cdgmm': (_c_int, [_vp, _vp, _vp, ctypes.c_longlong, ctypes.c_longlong, _c_int, _vp]),
     'kym_op_modulus': (_c_int, [_vp, _vp, ctypes.c_longlong, _vp]),

@@ -64,29 +64,113 @@ __global__ void reflect_pad_adjoint_kernel(const float* __restrict__ gpad, long 
 }
 
 // One block per (strip of kGatherRows rows x tile of blockDim columns, task,
-// image); one thread per column.  The task's gather list is staged in shared memory
-// kGatherMax items at a time; per child the column residue is one division
-// and the row residue advances incrementally.
-constexpr int kGatherRows = 8;
+// image); one thread per column.  The kernel is bound by load latency, so the
+// loads of kGatherUnroll children are issued before their products are
+// summed.  The column residues v mod (mc / 2^q) and the strip's row residues
+// are tabulated once per block (a child costs a table lookup instead of two
+// divisions), and the task's gather list is staged in shared memory
+// kGatherMax items at a time.
 constexpr int kGatherMax = 64;
 
-__global__ void bwd_gather_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather,
+__global__ void __launch_bounds__(kGatherThreads) bwd_gather_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather,
                                   FilterTable F, int mr, int mc, float2* __restrict__ gy, long long gy_stride,
-                                  const float2* __restrict__ gyc, long long gyc_stride) {
+                                  const float2* __restrict__ gyc, long long gyc_stride, int nimg) {
+  constexpr int R = kGatherRows, CU = kGatherUnroll;
   __shared__ GatherItem items[kGatherMax];
+  __shared__ int vres[kGatherLogs][kGatherThreads];
+  __shared__ int ures[kGatherLogs];
   const BwdTask t = tasks[blockIdx.y];
-  if (t.gather_count == 0) return;
-  const size_t img = blockIdx.z;
-  const float2* yc = gyc + img * gyc_stride;
-  float2* out = gy + img * gy_stride + t.gy_off;
+  if (t.gather_count == 0 || (int)blockIdx.z >= nimg) return;
+  const float2* yc = gyc + (size_t)blockIdx.z * gyc_stride;
   // blockIdx.x = strip * column tiles + tile (long 1-D rows span several tiles)
   const int ctiles = (mc + blockDim.x - 1) / blockDim.x;
-  const int u0 = (blockIdx.x / ctiles) * kGatherRows;
-  const int u1 = min(u0 + kGatherRows, mr);
+  const int u0 = (blockIdx.x / ctiles) * R;
+  const int nr = min(R, mr - u0);
   const int v = (blockIdx.x % ctiles) * blockDim.x + threadIdx.x;
-  float2 acc[kGatherRows];
+#pragma unroll 1
+  for (int q = 0; q < kGatherLogs; ++q) {
+    const int m = mc >> q;
+    vres[q][threadIdx.x] = m > 0 ? v % m : 0;
+  }
+  if (threadIdx.x < kGatherLogs) {
+    const int m = mr >> threadIdx.x;
+    ures[threadIdx.x] = m > 0 ? u0 % m : 0;
+  }
+  float2 acc[R];
 #pragma unroll
-  for (int r = 0; r < kGatherRows; ++r) acc[r] = make_float2(0.f, 0.f);
+  for (int r = 0; r < R; ++r) acc[r] = make_float2(0.f, 0.f);
+  for (int c0 = 0; c0 < t.gather_count; c0 += kGatherMax) {
+    const int nc = min(t.gather_count - c0, kGatherMax);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) items[i] = gather[t.gather_first + c0 + i];
+    __syncthreads();
+    if (v >= mc) continue;
+    for (int c = 0; c < nc; c += CU) {
+      float f[CU][R];
+      float2 y[CU][R];
+#pragma unroll
+      for (int k = 0; k < CU; ++k) {
+        const bool live = c + k < nc;  // uniform over the block
+        const GatherItem& gi = items[live ? c + k : c];
+        const float* psi = F.f[gi.psi] + (size_t)u0 * mc + v;
+        const float2* ycol = yc + gi.gy_off + vres[gi.lkc][threadIdx.x];
+        int um = ures[gi.lkr];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const bool ok = live && r < nr;
+          f[k][r] = ok ? __ldg(psi + (size_t)r * mc) * gi.w : 0.f;
+          y[k][r] = ok ? __ldg(ycol + (size_t)um * gi.mc) : make_float2(0.f, 0.f);
+          if (++um == gi.mr) um = 0;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < CU; ++k)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          acc[r].x = fmaf(y[k][r].x, f[k][r], acc[r].x);
+          acc[r].y = fmaf(y[k][r].y, f[k][r], acc[r].y);
+        }
+    }
+  }
+  if (v < mc) {
+    float2* out = gy + (size_t)blockIdx.z * gy_stride + t.gy_off;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (r < nr) out[(size_t)(u0 + r) * mc + v] = acc[r];
+  }
+}
+
+template <int NP>
+__global__ void __launch_bounds__(kGatherThreads)
+    bwd_gather_set_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather, FilterTable F,
+                          int mr, int mc, float2* __restrict__ gy, long long gy_stride,
+                          const float2* __restrict__ gyc, long long gyc_stride, int nimg) {
+  constexpr int R = kGatherSetRows;
+  __shared__ GatherItem items[kGatherMax];
+  __shared__ int vres[kGatherLogs][kGatherThreads];
+  __shared__ int ures[kGatherLogs];
+  const int first = blockIdx.y * NP;  // the set's first task carries the gather list
+  const BwdTask t = tasks[first];
+  if (t.gather_count == 0 || (int)blockIdx.z >= nimg) return;
+  const float2* yc = gyc + (size_t)blockIdx.z * gyc_stride;
+  const int ctiles = (mc + blockDim.x - 1) / blockDim.x;
+  const int u0 = (blockIdx.x / ctiles) * R;
+  const int nr = min(R, mr - u0);
+  const int v = (blockIdx.x % ctiles) * blockDim.x + threadIdx.x;
+#pragma unroll 1
+  for (int q = 0; q < kGatherLogs; ++q) {
+    const int m = mc >> q;
+    vres[q][threadIdx.x] = m > 0 ? v % m : 0;
+  }
+  if (threadIdx.x < kGatherLogs) {
+    const int m = mr >> threadIdx.x;
+    ures[threadIdx.x] = m > 0 ? u0 % m : 0;
+  }
+  float2 acc[NP][R];
+#pragma unroll
+  for (int p = 0; p < NP; ++p)
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[p][r] = make_float2(0.f, 0.f);
   for (int c0 = 0; c0 < t.gather_count; c0 += kGatherMax) {
     const int nc = min(t.gather_count - c0, kGatherMax);
     __syncthreads();
@@ -94,27 +178,47 @@ __global__ void bwd_gather_kernel(const BwdTask* __restrict__ tasks, const Gathe
     __syncthreads();
     if (v >= mc) continue;
     for (int c = 0; c < nc; ++c) {
-      const GatherItem gi = items[c];
-      const float* psi = F.f[gi.psi];
-      const float w = 1.f / (float)(gi.kr * gi.kc);
-      const float2* ycol = yc + gi.gy_off + (v % gi.mc);
-      int um = u0 % gi.mr;
+      const GatherItem& gi = items[c];
+      const float* psi = F.f[gi.psi] + (size_t)u0 * mc + v;
+      const float2* ycol = yc + gi.gy_off + vres[gi.lkc][threadIdx.x];
+      int um = ures[gi.lkr];
+      float f[R];
+      size_t yo[R];
 #pragma unroll
-      for (int r = 0; r < kGatherRows; ++r) {
-        if (u0 + r < u1) {
-          const float f = __ldg(psi + (size_t)(u0 + r) * mc + v) * w;
-          const float2 y = __ldg(ycol + (size_t)um * gi.mc);
-          acc[r].x = fmaf(y.x, f, acc[r].x);
-          acc[r].y = fmaf(y.y, f, acc[r].y);
-        }
+      for (int r = 0; r < R; ++r) {
+        f[r] = r < nr ? __ldg(psi + (size_t)r * mc) * gi.w : 0.f;
+        yo[r] = (size_t)um * gi.mc;
         if (++um == gi.mr) um = 0;
+      }
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const float2* yp = ycol + (size_t)p * gi.gy_pstride;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const float2 y = r < nr ? __ldg(yp + yo[r]) : make_float2(0.f, 0.f);
+          acc[p][r].x = fmaf(y.x, f[r], acc[p][r].x);
+          acc[p][r].y = fmaf(y.y, f[r], acc[p][r].y);
+        }
       }
     }
   }
-  if (v < mc)
+  if (v < mc) {
 #pragma unroll
-    for (int r = 0; r < kGatherRows; ++r)
-      if (u0 + r < u1) out[(size_t)(u0 + r) * mc + v] = acc[r];
+    for (int p = 0; p < NP; ++p) {
+      float2* out = gy + (size_t)blockIdx.z * gy_stride + tasks[first + p].gy_off;
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (r < nr) out[(size_t)(u0 + r) * mc + v] = acc[p][r];
+    }
+  }
+}
+
+cudaError_t launch_gather_set(int np, dim3 grid, int threads, cudaStream_t stream, const BwdTask* tasks,
+                              const GatherItem* gather, const FilterTable& F, int mr, int mc, float2* gy,
+                              long long gy_stride, const float2* gyc, long long gyc_stride, int nimg) {
+  auto kern = np == 8 ? bwd_gather_set_kernel<8> : np == 4 ? bwd_gather_set_kernel<4> : bwd_gather_set_kernel<2>;
+  kern<<<grid, threads, 0, stream>>>(tasks, gather, F, mr, mc, gy, gy_stride, gyc, gyc_stride, nimg);
+  return cudaGetLastError();
 }
 
 namespace {

@@ -30,15 +30,17 @@ struct BwdTask {
   int out_ch;         // channel of the incoming gradient
   int gather_first;   // children in the gather table
   int gather_count;
-  int pad_;
+  int y_off;          // saved modulus input y within one image's saved block (levels 1, 2)
 };
 
 struct GatherItem {
   long long gy_off;  // child's g_Y within one image's child block
   int psi;           // child's wavelet at the parent's resolution
   int mr, mc;        // child's work size
-  int kr, kc;        // fold factor parent -> child
+  int lkr, lkc;      // log2 of the fold factors parent -> child (powers of two)
+  float w;           // 1 / (kr kc)
   int pad_;
+  long long gy_pstride;  // parent sets: the same child of the next parent of the set is gy_pstride further
 };
 
 struct BwdLaunch {
@@ -62,6 +64,8 @@ struct BwdLaunch {
   const GatherItem* gather;
   int img0;
   const float2* tw_rl;  // local column length of a cluster split (mr / cluster)
+  const float2* ysaved;  // non-null: y saved by the forward, read instead of recomputed
+  long long ysaved_stride;
 };
 
 // ---------------------------------------------------------------------------
@@ -242,28 +246,39 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
   // levels 1 and 2 keep g_U in this CTA's (possibly permuted) rows
   for (int i = threadIdx.x; i < nloc; i += NT) gu_out[i] = at(i / MC, i % MC)->x;
 
-  // 4. recompute y = IFFT2(fold(P * psi)) for the modulus phase
+  // 4. y = IFFT2(fold(P * psi)) for the modulus phase: saved by the forward
+  // (natural rows), or recomputed from the parent spectrum
   __syncthreads();  // g_U stores visible to this CTA before they are re-read in step 5
-  const float2* src = L.src + (size_t)img * L.src_stride + t.src_off;
-  const float* psi = F.f[t.psi];
-  const int scols = L.kc * MC;
-  for (int i = threadIdx.x; i < nloc; i += NT) {
-    const int u = i / MC, v = i % MC;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int a = 0; a < L.kr; ++a) {
-      const size_t rb = (size_t)(row0 + u + a * MR) * scols + v;
-      for (int b = 0; b < L.kc; ++b) {
-        const size_t idx = rb + (size_t)b * MC;
-        const float2 s = __ldg(src + idx);
-        const float w = __ldg(psi + idx);
-        acc.x = fmaf(s.x, w, acc.x);
-        acc.y = fmaf(s.y, w, acc.y);
-      }
+  if (L.ysaved) {
+    const float2* ys = L.ysaved + (size_t)img * L.ysaved_stride + t.y_off;
+    for (int i = threadIdx.x; i < nloc; i += NT) {
+      const int u = i / MC, v = i % MC;
+      const int grow = E::kPerm ? e.rank + L.cluster * u : row0 + u;
+      *at(u, v) = __ldg(ys + (size_t)grow * MC + v);
     }
-    *at(u, v) = cscale(acc, L.rec_scale);
+    __syncthreads();
+  } else {
+    const float2* src = L.src + (size_t)img * L.src_stride + t.src_off;
+    const float* psi = F.f[t.psi];
+    const int scols = L.kc * MC;
+    for (int i = threadIdx.x; i < nloc; i += NT) {
+      const int u = i / MC, v = i % MC;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int a = 0; a < L.kr; ++a) {
+        const size_t rb = (size_t)(row0 + u + a * MR) * scols + v;
+        for (int b = 0; b < L.kc; ++b) {
+          const size_t idx = rb + (size_t)b * MC;
+          const float2 s = __ldg(src + idx);
+          const float w = __ldg(psi + idx);
+          acc.x = fmaf(s.x, w, acc.x);
+          acc.y = fmaf(s.y, w, acc.y);
+        }
+      }
+      *at(u, v) = cscale(acc, L.rec_scale);
+    }
+    __syncthreads();
+    e.fft2_dif(true);
   }
-  __syncthreads();
-  e.fft2_dif(true);
 
   // 5. g_y = g_U * y / |y|  (zero where |y| == 0)
   for (int i = threadIdx.x; i < nloc; i += NT) {
@@ -317,10 +332,24 @@ __global__ void __launch_bounds__(kThreads, 1)
 // Children's contributions to a parent's spectrum gradient:
 //   out[img][task][u][v] = sum_c psi_c[u][v] * g_Y_c[u mod mr_c][v mod mc_c] / (kr_c kc_c)
 // written into each task's gradient block (complex, mr x mc).  One thread
-// per element; grid = (element blocks, tasks, images).
-__global__ void bwd_gather_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather,
+// per column of a strip of kGatherRows rows; grid = (strips x column tiles,
+// tasks, images).
+constexpr int kGatherRows = 4;
+constexpr int kGatherUnroll = 4;  // children whose loads are in flight together
+constexpr int kGatherThreads = 256;
+constexpr int kGatherLogs = 24;  // fold factors up to 2^23
+// Parent sets: NP consecutive tasks whose children use the same wavelets and
+// geometry (the L orientations theta1 of one scale j1, whose children are
+// the same (j2, theta2) paths) are gathered by one block, so each wavelet
+// value is loaded once for the NP parents; strips of kGatherSetRows rows.
+constexpr int kGatherSetRows = 2;
+// np in {2, 4, 8}; grid = (strips x column tiles, sets, images)
+cudaError_t launch_gather_set(int np, dim3 grid, int threads, cudaStream_t stream, const BwdTask* tasks,
+                              const GatherItem* gather, const FilterTable& F, int mr, int mc, float2* gy,
+                              long long gy_stride, const float2* gyc, long long gyc_stride, int nimg);
+__global__ void __launch_bounds__(kGatherThreads) bwd_gather_kernel(const BwdTask* __restrict__ tasks, const GatherItem* __restrict__ gather,
                                   FilterTable F, int mr, int mc, float2* __restrict__ gy, long long gy_stride,
-                                  const float2* __restrict__ gyc, long long gyc_stride);
+                                  const float2* __restrict__ gyc, long long gyc_stride, int nimg);
 
 // Reflect-pad adjoint: g_x[i][j] = sum of g_pad over the padded positions that
 // reflect onto (i, j) (kymatio/scattering2d/backend/torch_backend.py:56-57,

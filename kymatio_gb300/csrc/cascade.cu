@@ -120,10 +120,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       if constexpr (CL) cg::this_cluster().sync();
       fft_pass<false, false, CL>(w, cpc, rank * cpc, L.pcol, true, wide_bar);
     }
+    float2* ys = (L.ysave && t.y_off >= 0) ? L.ysave + (size_t)img * L.ysave_stride + t.y_off : nullptr;
     for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
       const int u = e / mc, v = e - (e / mc) * mc;
       float2* p = elem(u, v);
       const float2 z = *p;
+      if (ys) ys[(size_t)(row0 + u) * mc + v] = z;  // saved for the backward
       *p = make_float2(sqrtf(z.x * z.x + z.y * z.y), 0.f);
     }
     if constexpr (!ONED) {
@@ -254,6 +256,7 @@ struct BwdGroup {
   bool has_ct = false;
   size_t smem = 0;             // shared memory of the launched variant
   BwdCtLauncher ct = nullptr;
+  int gather_np = 1;           // parents per gather block (sets of tasks sharing their children's wavelets)
 };
 
 struct CascadePlan {
@@ -446,6 +449,7 @@ struct RunArgs {
   bool stage0_per_chunk = false;
   float* group_ms = nullptr;
   int max_groups = 0;
+  float2* ysave = nullptr;  // non-null: every path stores its modulus input (per image gy2 + gy1 elements)
 };
 
 static int fail_cuda(cudaError_t e, const char* what) {
@@ -501,6 +505,10 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
       L.x_stride = x_stride;
       L.out = out;
       L.out_stride = out_stride;
+      if (a.ysave && g.level > 0) {
+        L.ysave = a.ysave + (size_t)c0 * (P->gy1_elems + P->gy2_elems);
+        L.ysave_stride = P->gy1_elems + P->gy2_elems;
+      }
       int n = nimg;
       // image c of the chunk has its input spectrum at u0 + i * u0_elems, with
       // i = c0 + c when the input stage covers the whole batch, i = c otherwise
@@ -528,6 +536,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
         Li.img0 = L.img0 + i0;
         if (Li.src) Li.src = L.src + (size_t)i0 * L.src_stride;
         if (Li.dst) Li.dst = L.dst + (size_t)i0 * L.dst_stride;
+        if (Li.ysave) Li.ysave = L.ysave + (size_t)i0 * L.ysave_stride;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (timed && (int)gi < a.max_groups) {
           cudaEventCreate(&e0);
@@ -569,7 +578,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
 static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
                     int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
                     float* group_ms = nullptr, int max_groups = 0, const LowpassTable* lp = nullptr,
-                    unsigned* status = nullptr) {
+                    unsigned* status = nullptr, float2* ysave = nullptr) {
   if (!P || !x || !out || batch < 0) {
     set_error_message("forward", "null plan, input or output");
     return KYM_ERR_INVALID;
@@ -593,8 +602,9 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   a.chunk = chunk;
   a.group_ms = group_ms;
   a.max_groups = max_groups;
-  a.lp = lp;
+  a.lp = ysave ? nullptr : lp;  // the tensor-core kernels do not save y
   a.status = status;
+  a.ysave = ysave;
   return run_core(P, x, out, batch, F, a, stream);
 }
 
@@ -712,11 +722,26 @@ static int build_backward(CascadePlan* P) {
     it.psi = c.tasks[ti].psi;
     it.mr = c.L.mr;
     it.mc = c.L.mc;
-    it.kr = c.L.kr;
-    it.kc = c.L.kc;
+    auto lg = [](int k) {
+      int q = 0;
+      while ((1 << q) < k) ++q;
+      return q;
+    };
+    it.lkr = lg(c.L.kr);
+    it.lkc = lg(c.L.kc);
+    it.w = (float)(1.0 / ((double)c.L.kr * c.L.kc));
     it.pad_ = 0;
+    it.gy_pstride = 0;
     return it;
   };
+  // the gather tabulates residues for power-of-two folds only (every fold of
+  // the 1-D and 2-D cascades is one)
+  for (const Group& g : P->groups)
+    if ((g.L.kr & (g.L.kr - 1)) || (g.L.kc & (g.L.kc - 1)) || g.L.kr >= (1 << kGatherLogs) ||
+        g.L.kc >= (1 << kGatherLogs)) {
+      set_error_message("plan", "fold factor is not a power of two below 2^24");
+      return KYM_ERR_UNSUPPORTED;
+    }
   for (int level : {2, 1, 0}) {
     for (size_t gi = 0; gi < P->groups.size(); ++gi) {
       const Group& g = P->groups[gi];
@@ -734,7 +759,7 @@ static int build_backward(CascadePlan* P) {
         bt.out_ch = t.out_ch;
         bt.gather_first = (int)P->all_gather.size();
         bt.gather_count = 0;
-        bt.pad_ = 0;
+        bt.y_off = level == 0 ? -1 : (int)(gy_of[gi][ti] + (level == 1 ? P->gy2_elems : 0));
         if (level == 1 && t.dst_off >= 0) {
           auto it = children.find(t.dst_off);
           if (it != children.end())
@@ -757,12 +782,51 @@ static int build_backward(CascadePlan* P) {
       } else {
         b.smem = rt_bwd_smem(g.L);
       }
+      // parent sets for the gather: NP consecutive tasks with the same
+      // children wavelets and geometry, each child's g_Y a fixed stride
+      // further for the next parent of the set
+      for (int np : {8, 4, 2}) {
+        const int nt = (int)b.tasks.size();
+        if (nt % np || b.tasks[0].gather_count == 0) continue;
+        bool ok = true;
+        std::vector<long long> stride(b.tasks[0].gather_count, 0);
+        for (int s0 = 0; s0 < nt && ok; s0 += np) {
+          const BwdTask& a = b.tasks[s0];
+          for (int p = 1; p < np && ok; ++p) {
+            const BwdTask& q = b.tasks[s0 + p];
+            ok = q.gather_count == a.gather_count;
+            for (int i = 0; ok && i < a.gather_count; ++i) {
+              const GatherItem& x = P->all_gather[a.gather_first + i];
+              const GatherItem& y = P->all_gather[q.gather_first + i];
+              const long long d = y.gy_off - x.gy_off;
+              if (p == 1 && s0 == 0) stride[i] = d;
+              ok = y.psi == x.psi && y.mr == x.mr && y.mc == x.mc && y.lkr == x.lkr && y.lkc == x.lkc &&
+                   d == (long long)p * stride[i] && stride[i] > 0;
+            }
+          }
+        }
+        if (!ok) continue;
+        b.gather_np = np;
+        for (int s0 = 0; s0 < nt; s0 += np)
+          for (int i = 0; i < b.tasks[s0].gather_count; ++i) P->all_gather[b.tasks[s0].gather_first + i].gy_pstride = stride[i];
+        break;
+      }
       b.task_off = P->all_btasks.size();
       P->all_btasks.insert(P->all_btasks.end(), b.tasks.begin(), b.tasks.end());
       P->bgroups.push_back(b);
     }
   }
-  const double budget = 256.0 * 1024 * 1024;
+  // the forward tasks store y (the saved-activation form) at the same offsets:
+  // per image [order-2 block | order-1 block]
+  for (size_t gi = 0; gi < P->groups.size(); ++gi) {
+    Group& g = P->groups[gi];
+    for (size_t ti = 0; ti < g.tasks.size(); ++ti) {
+      const int y = g.level == 0 ? -1 : (int)(gy_of[gi][ti] + (g.level == 1 ? P->gy2_elems : 0));
+      g.tasks[ti].y_off = y;
+      P->all_tasks[g.task_off + ti].y_off = y;
+    }
+  }
+  const double budget = 1024.0 * 1024 * 1024;  // backward workspace per pass
   const double per = (double)(P->u0_elems + P->u1_elems + P->gy1_elems + P->gy2_elems) * sizeof(float2);
   P->bchunk = (int)std::max(1.0, std::min(budget / per, (double)(1 << 20)));
   return KYM_OK;
@@ -810,8 +874,8 @@ static cudaError_t launch_rt_bwd(const BwdGroup& b, const BwdLaunch& L, const Fi
 // reflect-pad adjoint.
 static int run_backward(CascadePlan* P, const float* x, const float* gout, float* gx, int batch,
                         const float* const* filters, int nfilters, void* workspace, size_t ws_bytes,
-                        cudaStream_t stream) {
-  if (!P || !x || !gout || !gx || batch < 0) {
+                        cudaStream_t stream, const float2* ysaved = nullptr) {
+  if (!P || (!x && !ysaved) || !gout || !gx || batch < 0) {
     set_error_message("backward", "null plan, input, gradient or output");
     return KYM_ERR_INVALID;
   }
@@ -836,7 +900,9 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
   cudaError_t err = cudaSuccess;
   for (int c0 = 0; c0 < batch; c0 += chunk) {
     const int nimg = std::min(chunk, batch - c0);
-    // 1. recompute the spectra the backward needs (input stage, parents)
+    const long long ystride = P->gy1_elems + P->gy2_elems;
+    // 1. recompute the spectra the backward needs (input stage, parents),
+    // unless the forward saved every path's modulus input
     RunArgs a;
     a.ds = ds;
     a.u0 = u0;
@@ -848,7 +914,7 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
       bool needed = g.level == 0;
       if (g.level == 1)
         for (const Task& t : g.tasks) needed |= t.dst_off >= 0;
-      if (!needed) continue;
+      if (!needed || ysaved) continue;
       CascadeLaunch L = g.L;
       L.tasks = ds->tasks + g.task_off;
       L.ntasks = (int)g.tasks.size();
@@ -915,6 +981,10 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
       L.ntasks = (int)b.tasks.size();
       L.gather = ds->gather;
       L.img0 = c0;
+      if (ysaved && b.level > 0) {
+        L.ysaved = ysaved + (size_t)c0 * ystride;
+        L.ysaved_stride = ystride;
+      }
       if (b.level == 2) {
         L.src = u1;
         L.src_stride = P->u1_elems;
@@ -936,11 +1006,20 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
       bool any_gather = false;
       for (const BwdTask& bt : b.tasks) any_gather |= bt.gather_count > 0;
       if (any_gather) {
-        const int threads = std::min(512, (L.mc + 31) / 32 * 32);  // one thread per column
+        // one thread per column, at most kGatherThreads per block, tiles of equal width
+        const int ntile = (L.mc + kGatherThreads - 1) / kGatherThreads;
+        const int threads = ((L.mc + ntile - 1) / ntile + 31) / 32 * 32;
         const int ctiles = (L.mc + threads - 1) / threads;
-        dim3 grid((L.mr + 7) / 8 * ctiles, L.ntasks, nimg);
-        bwd_gather_kernel<<<grid, threads, 0, stream>>>(L.tasks, L.gather, F, L.mr, L.mc, L.gy, L.gy_stride, L.gyc,
-                                                      L.gyc_stride);
+        if (b.gather_np > 1) {
+          dim3 grid((L.mr + kGatherSetRows - 1) / kGatherSetRows * ctiles, L.ntasks / b.gather_np, nimg);
+          err = launch_gather_set(b.gather_np, grid, threads, stream, L.tasks, L.gather, F, L.mr, L.mc, L.gy,
+                                  L.gy_stride, L.gyc, L.gyc_stride, nimg);
+          if (err != cudaSuccess) return fail_cuda(err, "backward gather");
+        } else {
+          dim3 grid((L.mr + kGatherRows - 1) / kGatherRows * ctiles, L.ntasks, nimg);
+          bwd_gather_kernel<<<grid, threads, 0, stream>>>(L.tasks, L.gather, F, L.mr, L.mc, L.gy, L.gy_stride, L.gyc,
+                                                        L.gyc_stride, nimg);
+        }
         err = cudaGetLastError();
         if (err != cudaSuccess) return fail_cuda(err, "backward gather");
       }
@@ -961,6 +1040,32 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
     if (err != cudaSuccess) return fail_cuda(err, "reflect-pad adjoint");
   }
   return KYM_OK;
+}
+
+static size_t saved_bytes(const CascadePlan* P, int batch) {
+  return (size_t)batch * (P->gy1_elems + P->gy2_elems) * sizeof(float2);
+}
+
+static int run_forward_save(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
+                            int nfilters, void* workspace, size_t ws_bytes, void* saved, size_t saved_size,
+                            cudaStream_t stream) {
+  if (batch > 0 && (!saved || saved_size < saved_bytes(P, batch))) {
+    set_error_message("forward_save", "saved-activation buffer missing or smaller than the plan requires");
+    return KYM_ERR_WORKSPACE;
+  }
+  return run_plan(P, x, out, batch, filters, nfilters, workspace, ws_bytes, stream, nullptr, 0, nullptr, nullptr,
+                  static_cast<float2*>(saved));
+}
+
+static int run_backward_saved(CascadePlan* P, const void* saved, size_t saved_size, const float* gout, float* gx,
+                              int batch, const float* const* filters, int nfilters, void* workspace,
+                              size_t ws_bytes, cudaStream_t stream) {
+  if (batch > 0 && (!saved || saved_size < saved_bytes(P, batch))) {
+    set_error_message("backward_saved", "saved-activation buffer missing or smaller than the plan requires");
+    return KYM_ERR_WORKSPACE;
+  }
+  return run_backward(P, nullptr, gout, gx, batch, filters, nfilters, workspace, ws_bytes, stream,
+                      static_cast<const float2*>(saved));
 }
 
 static void set_default_chunk(CascadePlan* P) {
@@ -1052,7 +1157,7 @@ extern "C" int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, in
     g.L.img_N = P->img_N;
     g.L.pad_t = P->pad_t;
     g.L.pad_l = P->pad_l;
-    g.tasks.push_back(Task{0, 0, -1, 0, 0, 0});
+    g.tasks.push_back(Task{0, 0, -1, 0, 0, -1});
     P->groups.push_back(g);
   }
   // order 1, one launch per scale
@@ -1067,7 +1172,7 @@ extern "C" int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, in
     g.L.out_nc = P->out_nc;
     for (int t = 0; t < L; ++t) {
       const int n1 = j1 * L + t;
-      g.tasks.push_back(Task{0, u1_off[n1], psi_first[n1], j1, 1 + n1, 0});
+      g.tasks.push_back(Task{0, u1_off[n1], psi_first[n1], j1, 1 + n1, -1});
     }
     P->groups.push_back(g);
   }
@@ -1094,7 +1199,7 @@ extern "C" int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, in
           byscale[key] = g;
           order.push_back(key);
         }
-        byscale[key].tasks.push_back(Task{u1_off[n1], -1, psi_first[n2] + j1, j2, ch++, 0});
+        byscale[key].tasks.push_back(Task{u1_off[n1], -1, psi_first[n2] + j1, j2, ch++, -1});
       }
     }
     for (auto& key : order) P->groups.push_back(byscale[key]);
@@ -1233,6 +1338,27 @@ extern "C" int kym_s2d_backward(const kym_s2d_plan* plan, const float* x, const 
                            workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
 }
 
+extern "C" size_t kym_s2d_saved_bytes(const kym_s2d_plan* plan, int batch) {
+  if (!plan || batch < 0) return 0;
+  return kym::saved_bytes(&plan->p, batch);
+}
+
+extern "C" int kym_s2d_forward_save(const kym_s2d_plan* plan, const float* x, float* out, int batch,
+                                    const float* const* filters, int n_filters, void* workspace,
+                                    size_t workspace_bytes, void* saved, size_t saved_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_forward_save(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
+                               workspace_bytes, saved, saved_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int kym_s2d_backward_saved(const kym_s2d_plan* plan, const void* saved, size_t saved_bytes,
+                                      const float* grad_out, float* grad_x, int batch, const float* const* filters,
+                                      int n_filters, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_backward_saved(const_cast<CascadePlan*>(&plan->p), saved, saved_bytes, grad_out, grad_x, batch,
+                                 filters, n_filters, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
 extern "C" int kym_s2d_forward(const kym_s2d_plan* plan, const float* x, float* out, int batch,
                                const float* const* filters, int n_filters, void* workspace,
                                size_t workspace_bytes, void* stream) {
@@ -1335,7 +1461,7 @@ extern "C" int kym_s1d_plan_create(int N_padded, int N_input, int pad_left, int 
     Group* g = group_for(0, N_padded, 1, false, true);
     if (!g) { rc = KYM_ERR_UNSUPPORTED; goto fail; }
     // phi level 0 with the input stage; fold factor 2^log2_stride for S
-    g->tasks.push_back(Task{0, 0, -1, phi_idx[0], ch++, 0});
+    g->tasks.push_back(Task{0, 0, -1, phi_idx[0], ch++, -1});
   }
   for (int n1 = 0; n1 < n_psi1; ++n1) {
     const int j1 = psi1_j[n1];
@@ -1350,7 +1476,7 @@ extern "C" int kym_s1d_plan_create(int N_padded, int N_input, int pad_left, int 
     if (k1 >= n_phi_levels) { rc = KYM_ERR_INVALID; goto fail; }
     Group* g = group_for(1, N_padded >> k1, 1 << k1, true, false);
     if (!g) { rc = KYM_ERR_UNSUPPORTED; goto fail; }
-    g->tasks.push_back(Task{0, u1_off[n1], psi1_first[n1], phi_idx[k1], ch++, 0});
+    g->tasks.push_back(Task{0, u1_off[n1], psi1_first[n1], phi_idx[k1], ch++, -1});
   }
   if (second) {
     for (int n1 = 0; n1 < n_psi1; ++n1) {
@@ -1364,7 +1490,7 @@ extern "C" int kym_s1d_plan_create(int N_padded, int N_input, int pad_left, int 
         if (k1 >= psi2_nlevels[n2] || k1 + k2 >= n_phi_levels) { rc = KYM_ERR_INVALID; goto fail; }
         Group* g = group_for(2, N_padded >> (k1 + k2), 1 << k2, true, false);
         if (!g) { rc = KYM_ERR_UNSUPPORTED; goto fail; }
-        g->tasks.push_back(Task{u1_off[n1], -1, psi2_first[n2] + k1, phi_idx[k1 + k2], ch++, 0});
+        g->tasks.push_back(Task{u1_off[n1], -1, psi2_first[n2] + k1, phi_idx[k1 + k2], ch++, -1});
       }
     }
   }
@@ -1422,6 +1548,27 @@ extern "C" int kym_s1d_backward(const kym_s1d_plan* plan, const float* x, const 
   if (!plan) return KYM_ERR_INVALID;
   return kym::run_backward(const_cast<CascadePlan*>(&plan->p), x, grad_out, grad_x, batch, filters, n_filters,
                            workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" size_t kym_s1d_saved_bytes(const kym_s1d_plan* plan, int batch) {
+  if (!plan || batch < 0) return 0;
+  return kym::saved_bytes(&plan->p, batch);
+}
+
+extern "C" int kym_s1d_forward_save(const kym_s1d_plan* plan, const float* x, float* out, int batch,
+                                    const float* const* filters, int n_filters, void* workspace,
+                                    size_t workspace_bytes, void* saved, size_t saved_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_forward_save(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
+                               workspace_bytes, saved, saved_bytes, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int kym_s1d_backward_saved(const kym_s1d_plan* plan, const void* saved, size_t saved_bytes,
+                                      const float* grad_out, float* grad_x, int batch, const float* const* filters,
+                                      int n_filters, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!plan) return KYM_ERR_INVALID;
+  return kym::run_backward_saved(const_cast<CascadePlan*>(&plan->p), saved, saved_bytes, grad_out, grad_x, batch,
+                                 filters, n_filters, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int kym_s1d_forward(const kym_s1d_plan* plan, const float* x, float* out, int batch,

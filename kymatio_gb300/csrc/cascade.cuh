@@ -29,7 +29,7 @@ struct Task {
   int psi;            // filter index multiplied before the fold, -1 if none
   int phi;            // low-pass filter index
   int out_ch;         // output channel
-  int pad_;
+  int y_off;          // this path's modulus input y within one image's saved block, -1 if none
 };
 
 struct CascadeLaunch {
@@ -59,6 +59,8 @@ struct CascadeLaunch {
   int img0;     // first image of this chunk (for x/out offsets)
   int skip_s;   // 1: stop after storing the spectrum (backward recomputation)
   const float2* tw_rl;  // exp(-2 pi i k / (mr / cluster)): local column length of a cluster split
+  float2* ysave;        // non-null: store y = IFFT2(...) before the modulus (saved for the backward)
+  long long ysave_stride;
 };
 
 }  // namespace kym

@@ -219,9 +219,12 @@ __global__ void __launch_bounds__(NT, 1)
     // U = |IFFT2(A)| ; A = FFT2(U)  (a cluster leaves U in permuted rows)
     ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, true);
     if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, true, true);
+    // y saved for the backward in natural rows (a cluster holds row rank + C u)
+    float2* ys = (L.ysave && t.y_off >= 0) ? L.ysave + (size_t)img * L.ysave_stride + t.y_off : nullptr;
     for (int e = threadIdx.x; e < NLOC; e += NT) {
       float2* p = at(e / MC, e % MC);
       const float2 z = *p;
+      if (ys) ys[(size_t)(C > 1 ? rank + C * (e / MC) : e / MC) * MC + e % MC] = z;
       *p = make_float2(sqrtf(fmaf(z.x, z.x, z.y * z.y)), 0.f);
     }
     __syncthreads();

@@ -18,7 +18,7 @@ import numpy as np
 import torch
 import torch.nn as nn
 
-from . import _lib
+from . import _autograd, _lib
 from .filter_bank import border_indices, filter_bank_1d, geometry_1d
 from .scattering2d import _Plan
 
@@ -245,7 +245,7 @@ class Scattering1D(nn.Module):
             raise TypeError('The input must be float32 (got %s).' % x.dtype)
         batch_shape = x.shape[:-1]
         xb = x.reshape((-1, x.shape[-1]))
-        S = _Scattering1DFn.apply(xb, self)
+        S = _autograd.CascadeFn.apply(xb, self)
         S = S.reshape(tuple(batch_shape) + tuple(S.shape[-2:]))
         if self.out_type == 'array':
             return S
@@ -274,6 +274,21 @@ class Scattering1D(nn.Module):
                                            ws.data_ptr(), ws_bytes, stream), 'kym_s1d_forward')
         return out
 
+    # -- saved-activation form (autograd) -----------------------------------
+    #: bytes of saved modulus inputs above which the backward recomputes them
+    activation_budget = _autograd.DEFAULT_ACTIVATION_BUDGET
+
+    def _saved_bytes(self, B):
+        return _lib.load().kym_s1d_saved_bytes(self._get_plan().h, B)
+
+    def _forward_save_raw(self, x):
+        """Forward that also keeps every path's modulus input."""
+        return _autograd.forward_save(_lib.load(), 's1d', self, self._get_plan(), x,
+                                      (x.shape[0], self._channels, self._out_len))
+
+    def _backward_saved_raw(self, saved, grad, x_shape):
+        return _autograd.backward_saved(_lib.load(), 's1d', self, self._get_plan(), saved, grad, x_shape)
+
     def _backward_raw(self, x, grad):
         """grad_x = J^T grad through kym_s1d_backward (hand-written adjoints)."""
         plan = self._get_plan()
@@ -290,15 +305,3 @@ class Scattering1D(nn.Module):
             _lib.check(lib.kym_s1d_backward(plan.h, x.data_ptr(), grad.data_ptr(), gx.data_ptr(), B, ptrs,
                                             self._n_filters, ws.data_ptr(), ws_bytes, stream), 'kym_s1d_backward')
         return gx
-
-class _Scattering1DFn(torch.autograd.Function):
-    @staticmethod
-    def forward(ctx, x, module):
-        ctx.module = module
-        ctx.save_for_backward(x)
-        return module._forward_raw(x)
-
-    @staticmethod
-    def backward(ctx, grad):
-        (x,) = ctx.saved_tensors
-        return ctx.module._backward_raw(x, grad.contiguous()), None

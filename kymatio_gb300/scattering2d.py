@@ -12,7 +12,7 @@ and torch's current stream; CPU tensors are rejected, there is no fallback.
 import torch
 import torch.nn as nn
 
-from . import _lib
+from . import _autograd, _lib
 from .filter_bank import filter_bank_2d, padded_size_2d, separable_lowpass
 
 
@@ -141,7 +141,7 @@ class Scattering2D(nn.Module):
             raise TypeError('The input must be float32 (got %s).' % input.dtype)
         batch_shape = input.shape[:-2]
         x = input.reshape((-1,) + tuple(input.shape[-2:]))
-        S = _Scattering2DFn.apply(x, self)
+        S = _autograd.CascadeFn.apply(x, self)
         S = S.reshape(tuple(batch_shape) + tuple(S.shape[-3:]))
         if self.out_type == 'array':
             return S
@@ -207,6 +207,22 @@ class Scattering2D(nn.Module):
                                             self._n_filters, ws.data_ptr(), ws_bytes, stream), 'kym_s2d_backward')
         return gx
 
+    # -- saved-activation form (autograd) -----------------------------------
+    #: bytes of saved modulus inputs above which the backward recomputes them
+    activation_budget = _autograd.DEFAULT_ACTIVATION_BUDGET
+
+    def _saved_bytes(self, B):
+        return _lib.load().kym_s2d_saved_bytes(self._get_plan().h, B)
+
+    def _forward_save_raw(self, x):
+        """Plain FP32 forward that also keeps every path's modulus input."""
+        plan = self._get_plan()
+        return _autograd.forward_save(_lib.load(), 's2d', self, plan, x,
+                                      (x.shape[0], self._channels) + self._out_hw)
+
+    def _backward_saved_raw(self, saved, grad, x_shape):
+        return _autograd.backward_saved(_lib.load(), 's2d', self, self._get_plan(), saved, grad, x_shape)
+
     def extra_repr(self):
         return 'J={}, shape={}, L={}, max_order={}, pre_pad={}, out_type={!r}'.format(
             self.J, self.shape, self.L, self.max_order, self.pre_pad, self.out_type)
@@ -223,16 +239,3 @@ class _Plan:
             self._destroy(self.h)
         except Exception:
             pass
-
-
-class _Scattering2DFn(torch.autograd.Function):
-    @staticmethod
-    def forward(ctx, x, module):
-        ctx.module = module
-        ctx.save_for_backward(x)
-        return module._forward_raw(x)
-
-    @staticmethod
-    def backward(ctx, grad):
-        (x,) = ctx.saved_tensors
-        return ctx.module._backward_raw(x, grad.contiguous()), None

@@ -1,7 +1,9 @@
-"""Hand-written backward (kym_s2d_backward / kym_s1d_backward) against the
-reference torch backend's autograd gradient (float64, captured in
-tests/golden/ref_grads.npz) and against FP64 central finite differences of
-the oracle.  Tolerance: relative L2 <= 1e-5."""
+"""Hand-written backward against the reference torch backend's autograd
+gradient (float64, captured in tests/golden/ref_grads.npz) and against FP64
+central finite differences of the oracle, in both policies: the saved form
+(kym_*_forward_save + kym_*_backward_saved, the default under the activation
+budget) and the recompute form (kym_*_backward, budget 0).  Tolerance:
+relative L2 <= 1e-5."""
 import json
 import os
 
@@ -30,32 +32,43 @@ def _grad(S, x, g, dev):
     return xt.grad.cpu().numpy()
 
 
+POLICIES = ['saved', 'recompute']
+
+
+def _policy(S, policy):
+    S.activation_budget = 0 if policy == 'recompute' else 4 << 30
+    return S
+
+
+@pytest.mark.parametrize('policy', POLICIES)
 @pytest.mark.parametrize('case', META['g2'], ids=lambda c: c['name'])
-def test_2d_grad_vs_reference_autograd(case):
+def test_2d_grad_vs_reference_autograd(case, policy):
     dev = _cuda()
     from kymatio_gb300 import Scattering2D
-    S = Scattering2D(case['J'], tuple(case['shape']), max_order=case['max_order'],
-                     pre_pad=case['pre_pad']).to(dev)
+    S = _policy(Scattering2D(case['J'], tuple(case['shape']), max_order=case['max_order'],
+                             pre_pad=case['pre_pad']).to(dev), policy)
     n = case['name']
     gx = _grad(S, D[n + '/x'], D[n + '/g'], dev)
     assert gx.shape == D[n + '/gx'].shape
     assert rel_l2(gx, D[n + '/gx']) <= 1e-5
 
 
+@pytest.mark.parametrize('policy', POLICIES)
 @pytest.mark.parametrize('case', META['g1'], ids=lambda c: c['name'])
-def test_1d_grad_vs_reference_autograd(case):
+def test_1d_grad_vs_reference_autograd(case, policy):
     dev = _cuda()
     from kymatio_gb300.scattering1d import Scattering1D
     kw = dict(case['kwargs'])
     if isinstance(kw.get('Q'), list):
         kw['Q'] = tuple(kw['Q'])
-    S = Scattering1D(**kw).to(dev)
+    S = _policy(Scattering1D(**kw).to(dev), policy)
     n = case['name']
     gx = _grad(S, D[n + '/x'], D[n + '/g'], dev)
     assert rel_l2(gx, D[n + '/gx']) <= 1e-5
 
 
-def test_2d_grad_vs_fp64_finite_differences():
+@pytest.mark.parametrize('policy', POLICIES)
+def test_2d_grad_vs_fp64_finite_differences(policy):
     """32x32, J=2: 64 random pixels, h=1e-6 central differences of <g, S(x)>
     on the FP64 oracle vs the GPU backward."""
     dev = _cuda()
@@ -64,7 +77,7 @@ def test_2d_grad_vs_fp64_finite_differences():
     from test_oracle_golden import fd_grad_2d
     rng = np.random.default_rng(3)
     x = rng.random((1, 32, 32)).astype(np.float32)
-    S = Scattering2D(2, (32, 32)).to(dev)
+    S = _policy(Scattering2D(2, (32, 32)).to(dev), policy)
     g = rng.standard_normal((1, 81, 8, 8)).astype(np.float32)
     gx = _grad(S, x, g, dev)
     pix = [(0, int(rng.integers(32)), int(rng.integers(32))) for _ in range(64)]
@@ -101,3 +114,54 @@ def test_cfg4_fwd_bwd_batch32():
     gx1 = _grad(S, x[5:6], g[5:6], dev)
     assert rel_l2(gx[5:6], gx1) <= 1e-6
     assert np.isfinite(gx).all()
+
+
+def test_budget_selects_policy_and_forms_agree():
+    """The autograd node saves the modulus inputs while batch x saved bytes
+    stays within activation_budget and recomputes above it; both forms give
+    the same gradient, and the saved forward gives the plain output."""
+    dev = _cuda()
+    from kymatio_gb300 import Scattering2D
+    torch.manual_seed(0)
+    S = Scattering2D(3, (64, 64)).to(dev)
+    x = torch.rand(6, 64, 64, device=dev)
+    g = torch.randn(6, 217, 8, 8, device=dev)
+    need = S._saved_bytes(6)
+    assert need == 6 * S._saved_bytes(1) > 0
+    calls = []
+    for budget in (need, need - 1):
+        S.activation_budget = budget
+        orig = (S._backward_saved_raw, S._backward_raw)
+        S._backward_saved_raw = lambda *a, o=orig[0]: calls.append('saved') or o(*a)
+        S._backward_raw = lambda *a, o=orig[1]: calls.append('recompute') or o(*a)
+        xt = x.clone().requires_grad_()
+        y = S(xt)
+        y.backward(g)
+        del S._backward_saved_raw, S._backward_raw
+        if budget == need:
+            gs, ys = xt.grad.clone(), y.detach().clone()
+        else:
+            gr = xt.grad.clone()
+    assert calls == ['saved', 'recompute']
+    with torch.no_grad():
+        y0 = S(x)
+    assert torch.equal(ys, y0)
+    assert rel_l2(gs.cpu().numpy(), gr.cpu().numpy()) <= 1e-6
+
+
+def test_saved_form_1d_cfg2_shape():
+    """1-D saved form at the 8192-sample, J=6, Q=(8,1), T=64 workload: the
+    gradient of one signal matches a batch-of-one recompute run."""
+    dev = _cuda()
+    from kymatio_gb300.scattering1d import Scattering1D
+    S = Scattering1D(6, 8192, Q=(8, 1), T=64).to(dev)
+    rng = np.random.default_rng(1)
+    x = torch.from_numpy(rng.standard_normal((4, 8192)).astype(np.float32)).to(dev)
+    y = S(x)
+    g = torch.from_numpy(rng.standard_normal(tuple(y.shape)).astype(np.float32)).to(dev)
+    xt = x.clone().requires_grad_()
+    S(xt).backward(g)
+    S.activation_budget = 0
+    x1 = x[2:3].clone().requires_grad_()
+    S(x1).backward(g[2:3])
+    assert rel_l2(xt.grad[2:3].cpu().numpy(), x1.grad.cpu().numpy()) <= 1e-6
