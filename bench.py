@@ -6,6 +6,7 @@ U[1,4] px, rescaled to [0,1]; seed 2), batch 64 per GPU.  One step = one
 forward over the batch.  Inputs are generated synthetically (no dataset).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --extra NAME      # one of the other workloads alone (profiling)
 
 --impl reference times the reference algorithm's CPU implementation (the
 numpy oracle port of kymatio's numpy backend, float32 arithmetic like the
@@ -213,23 +214,22 @@ def _time_ms(fn, steps, warmup, flush):
     return tot / steps
 
 
-def extras(dev, flush, steps=5, warmup=3):
-    """The other workloads: throughput at 32x32 J=2 (batch 128), 1-D N=8192
-    J=6 Q=(8,1) T=64 (batch 256), forward+backward / forward at 128x128 J=4
-    (batch 32), and the mixed 512-image batch of sides {32,64,128,256}."""
+def _extra_s2d_32(dev, flush, steps, warmup):
+    """32x32, J=2, batch 128, U[0,1) seed 0 (plain and tensor-core forms)."""
     import torch
     from kymatio_gb300 import Scattering2D
-    from kymatio_gb300.batching import MixedScattering2D, default_J
-    from kymatio_gb300.scattering1d import Scattering1D
-    res = {}
-    # 32x32, J=2, batch 128, U[0,1) seed 0
     x = torch.from_numpy(np.random.default_rng(0).random((128, 32, 32)).astype(np.float32)).to(dev)
     S = Scattering2D(2, (32, 32)).to(dev)
     ms = _time_ms(lambda: S(x), steps, warmup, flush)
     S.tensor_cores = True
     ms_tc = _time_ms(lambda: S(x), steps, warmup, flush)
-    res['scattering2d_32x32_J2_b128'] = {'img_s': 128 / ms * 1e3, 'img_s_tc': 128 / ms_tc * 1e3}
-    # 1-D: white noise plus a linear chirp, seed 1
+    return {'img_s': 128 / ms * 1e3, 'img_s_tc': 128 / ms_tc * 1e3}
+
+
+def _extra_s1d_8192(dev, flush, steps, warmup):
+    """1-D N=8192, J=6, Q=(8,1), T=64, batch 256: white noise plus a linear chirp, seed 1."""
+    import torch
+    from kymatio_gb300.scattering1d import Scattering1D
     rng = np.random.default_rng(1)
     N, B = 8192, 256
     t = np.arange(N)
@@ -239,8 +239,14 @@ def extras(dev, flush, steps=5, warmup=3):
     xs = torch.from_numpy(sig.astype(np.float32)).to(dev)
     S1 = Scattering1D(6, N, Q=(8, 1), T=64).to(dev)
     ms = _time_ms(lambda: S1(xs), steps, warmup, flush)
-    res['scattering1d_8192_J6_Q8_T64_b256'] = {'sig_s': B / ms * 1e3}
-    # 128x128, J=4, batch 32: forward vs forward + hand-written backward
+    return {'sig_s': B / ms * 1e3}
+
+
+def _extra_fwd_bwd_128(dev, flush, steps, warmup):
+    """128x128, J=4, batch 32 (U[0,1) seed 3, upstream N(0,1)): forward vs
+    forward + hand-written backward, saved and recompute policies."""
+    import torch
+    from kymatio_gb300 import Scattering2D
     rng = np.random.default_rng(3)
     x4 = torch.from_numpy(rng.random((32, 128, 128)).astype(np.float32)).to(dev)
     g4 = torch.from_numpy(rng.standard_normal((32, 417, 8, 8)).astype(np.float32)).to(dev)
@@ -254,11 +260,17 @@ def extras(dev, flush, steps=5, warmup=3):
     fwdbwd = _time_ms(fb, steps, warmup, flush)
     S4.activation_budget = 0  # recompute form: only x kept, spectra and y recomputed
     fwdbwd_rc = _time_ms(fb, steps, warmup, flush)
-    res['scattering2d_128x128_J4_b32_fwd_bwd'] = {
-        'fwd_ms': fwd, 'fwd_bwd_ms': fwdbwd, 'ratio': fwdbwd / fwd,
-        'policy': 'saved modulus inputs, %.1f MB (4 GiB budget)' % (S4._saved_bytes(32) / 1e6),
-        'fwd_bwd_ms_recompute': fwdbwd_rc, 'ratio_recompute': fwdbwd_rc / fwd}
-    # mixed batch: 512 images, sides drawn from {32,64,128,256}, seed 4
+    return {'fwd_ms': fwd, 'fwd_bwd_ms': fwdbwd, 'ratio': fwdbwd / fwd,
+            'policy': 'saved modulus inputs, %.1f MB (4 GiB budget)' % (S4._saved_bytes(32) / 1e6),
+            'fwd_bwd_ms_recompute': fwdbwd_rc, 'ratio_recompute': fwdbwd_rc / fwd}
+
+
+def _extra_mixed_512(dev, flush, steps, warmup):
+    """512 images, sides drawn from {32,64,128,256}, seed 4: per-size launches
+    vs one CUDA graph over grouped streams (plain and tensor-core forms)."""
+    import torch
+    from kymatio_gb300 import Scattering2D
+    from kymatio_gb300.batching import MixedScattering2D, default_J
     rng = np.random.default_rng(4)
     sides = rng.choice([32, 64, 128, 256], size=512)
     imgs = [torch.from_numpy(rng.random((s, s)).astype(np.float32)).to(dev) for s in sides]
@@ -272,10 +284,21 @@ def extras(dev, flush, steps=5, warmup=3):
     gr = _time_ms(lambda: mix.forward_grouped(xs), steps, warmup, flush)
     mixt = MixedScattering2D(list(xs), tensor_cores=True).to(dev)
     grt = _time_ms(lambda: mixt.forward_grouped(xs), steps, warmup, flush)
-    res['mixed_512_sides_32_64_128_256'] = {
-        'img_s_per_size_sequential': 512 / seq * 1e3, 'img_s_graph': 512 / gr * 1e3,
-        'img_s_graph_tc': 512 / grt * 1e3, 'counts': {str(s): len(v) for s, v in sorted(groups.items())}}
-    return res
+    return {'img_s_per_size_sequential': 512 / seq * 1e3, 'img_s_graph': 512 / gr * 1e3,
+            'img_s_graph_tc': 512 / grt * 1e3, 'counts': {str(s): len(v) for s, v in sorted(groups.items())}}
+
+
+EXTRAS = {
+    'scattering2d_32x32_J2_b128': _extra_s2d_32,
+    'scattering1d_8192_J6_Q8_T64_b256': _extra_s1d_8192,
+    'scattering2d_128x128_J4_b32_fwd_bwd': _extra_fwd_bwd_128,
+    'mixed_512_sides_32_64_128_256': _extra_mixed_512,
+}
+
+
+def extras(dev, flush, steps=5, warmup=3, names=None):
+    """The other workloads (all of EXTRAS, or the named ones)."""
+    return {n: f(dev, flush, steps, warmup) for n, f in EXTRAS.items() if names is None or n in names}
 
 
 def run_ours(args, world, rank, local):
@@ -471,6 +494,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-extras', action='store_true', help='skip the other workloads')
     ap.add_argument('--batch', type=int, default=64, help='images per GPU (64 is the benchmark workload)')
+    ap.add_argument('--extra', choices=sorted(EXTRAS), default=None,
+                    help='run only this other workload (for profiling) and print its JSON line')
     args = ap.parse_args()
     global BATCH
     BATCH = args.batch
@@ -478,6 +503,12 @@ def main():
     if args.impl == 'reference':
         world, rank = int(os.environ.get('WORLD_SIZE', '1')), int(os.environ.get('RANK', '0'))
         run_reference(args, world, rank)
+        return
+    if args.extra:
+        import torch
+        dev = torch.device('cuda', 0)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+        print(json.dumps({'extra': args.extra, **extras(dev, flush, args.steps, args.warmup, [args.extra])[args.extra]}))
         return
     world, rank, local = dist_init()
     run_ours(args, world, rank, local)
