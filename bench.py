@@ -320,10 +320,12 @@ def run_ours(args, world, rank, local):
     for g in range(ngroups):
         v = [ctypes.c_int() for _ in range(6)]
         lib.kym_s2d_group_info(plan.h, g, *[ctypes.byref(i) for i in v])
-        ginfo.append([i.value for i in v] + [lib.kym_s2d_group_uses_tc(plan.h, g)])
+        ginfo.append([i.value for i in v] + [lib.kym_s2d_group_uses_tc(plan.h, g),
+                                             lib.kym_s2d_group_kernels(plan.h, g, 1)])
     chunk = lib.kym_s2d_get_chunk(plan.h)
     n_chunks = -(-BATCH // min(chunk, BATCH))
-    launches_per_step = sum(1 if gi[0] == 0 else n_chunks for gi in ginfo)
+    # kernels of the tensor-core form per step: the input stage once, every other group once per chunk
+    launches_per_step = sum(gi[7] * (1 if gi[0] == 0 else n_chunks) for gi in ginfo)
     out = torch.empty((BATCH, S._channels) + S._out_hw, device=dev)
     ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, BATCH)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
@@ -414,15 +416,21 @@ def run_ours(args, world, rank, local):
     # ---- roofline of the dominant launch group of the tensor-core form -----------
     per_launch = [g_tc[g] / (1 if gi[0] == 0 else n_chunks) for g, gi in enumerate(ginfo)]
     dom = int(np.argmax(g_tc))
-    lvl, ntasks, rows, cols, fold, cl, uses_tc = ginfo[dom]
+    lvl, ntasks, rows, cols, fold, cl, uses_tc, nkern = ginfo[dom]
     imgs_per_launch = BATCH if lvl == 0 else min(chunk, BATCH)
     side_out = SIDE // 2 ** J
+    Mp = ((SIDE + 2 ** J) // 2 ** J + 1) * 2 ** J
+    # algorithmic bytes of one launch: every source spectrum once per image (an
+    # order-1 group reads the input spectrum, an order-2 group its ntasks / L
+    # parents), the output channels, the parent spectra an order-1 group
+    # writes, and the filters once per launch
     if lvl == 0:
         bytes_launch = imgs_per_launch * (4 * SIDE * SIDE + 8 * rows * cols + 4 * side_out ** 2)
     else:
         src = fold * fold * rows * cols
-        spill_w = 8 * rows * cols if (lvl == 1 and not uses_tc and rows > (272 >> (J - 1))) else 0
-        bytes_launch = imgs_per_launch * ntasks * (8 * src + 4 * side_out ** 2 + spill_w) + \
+        n_src = 1 if lvl == 1 else max(1, ntasks // L)
+        spill_w = ntasks * 8 * rows * cols if (lvl == 1 and not uses_tc and J > 1 and rows > (Mp >> (J - 1))) else 0
+        bytes_launch = imgs_per_launch * (n_src * 8 * src + ntasks * 4 * side_out ** 2 + spill_w) + \
             ntasks * (4 * src + 4 * rows * cols)
     dur_s = per_launch[dom] / 1e3
     peaks = {}
@@ -470,8 +478,10 @@ def run_ours(args, world, rank, local):
             'gpu_launches': launches_per_step * args.steps,
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s',
                          'frac': achieved / hbm_peak, 'traffic': traffic,
-                         'kernel': 'cascade group %d (level %d, %dx%d, fold %d, cluster %d, %d tasks%s)'
-                                   % (dom, lvl, rows, cols, fold, abs(cl), ntasks, ', tensor-core' if uses_tc else ''),
+                         'kernel': 'cascade group %d (level %d, %dx%d, fold %d, %d tasks%s)'
+                                   % (dom, lvl, rows, cols, fold, ntasks,
+                                      ', tensor-core' if uses_tc else
+                                      (', %d line-split kernels' % nkern if nkern > 1 else ', one fused kernel')),
                          'kernel_ms_per_launch': per_launch[dom],
                          'peak_source': 'measured' if 'hbm_gbs' in peaks else 'fallback'},
             'fp32_fft': {'gflop_per_img_5nlogn': flops_img / 1e9,

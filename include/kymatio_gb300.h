@@ -98,6 +98,11 @@ int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int
                        float* group_ms, int max_groups);
 /* 1 if launch group `group` runs a tensor-core variant in kym_s2d_forward_tc. */
 int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);
+/* Kernel launches that group `group` makes per chunk of images: 1 for a
+ * fused cascade kernel, 3 or 4 for the line-split passes of the sizes above
+ * one CTA (tensor_cores != 0: in kym_s2d_forward_tc).  No counterpart in the
+ * reference (profiling). */
+int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores);
 
 /* Hand-written backward: grad_x (batch, M, N) = (d forward / d x)^T grad_out,
  * grad_out shaped like the forward's output.  Replaces torch autograd through

@@ -47,6 +47,7 @@ SIGNATURES = {
     'kym_s2d_forward_tc': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, ctypes.POINTER(_vp),
                                     ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp, _vp,
                                     ctypes.POINTER(ctypes.c_float), _c_int]),
+    'kym_s2d_group_kernels': (_c_int, [_vp, _c_int, _c_int]),
     'kym_s2d_group_uses_tc': (_c_int, [_vp, _c_int]),
     'kym_tc_selftest': (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _vp, _vp]),
     'kym_s2d_group_count': (_c_int, [_vp]),

@@ -18,6 +18,7 @@
 #include "ct_cascade.cuh"
 #include "bwd.cuh"
 #include "tc_cascade.cuh"
+#include "lines.cuh"
 #include "plan_util.h"
 #include "errors.h"
 
@@ -227,6 +228,7 @@ struct Group {
   bool has_tc = false;   // a tensor-core variant exists (childless tasks only)
   size_t tc_smem = 0;
   TcLauncher tc = nullptr;
+  LinesLauncher lines = nullptr;  // line-split passes (sizes above one CTA, every task owns a slot)
   std::vector<Task> tasks;
   size_t task_off = 0;   // offset into the device task array
   size_t smem = 0;
@@ -300,9 +302,23 @@ struct CascadePlan {
 static int finalize_groups(CascadePlan* P) {
   size_t total = 0;
   for (auto& g : P->groups) {
+    // the line-split passes work in each task's spectrum slot
+    for (const Task& t : g.tasks)
+      if (t.dst_off < 0) g.lines = nullptr;
     g.task_off = total;
     total += g.tasks.size();
   }
+  // the folded low-pass blocks of a line-split order-1 group sit after each
+  // image's parent spectra (groups run one after the other: one region)
+  long long lp = 0;
+  for (auto& g : P->groups) {
+    g.L.bsum_off = -1;
+    if (g.lines && g.L.modulus && g.level == 1) {
+      g.L.bsum_off = P->u1_elems;
+      lp = std::max(lp, (long long)g.tasks.size() * g.L.sr * g.L.sc);
+    }
+  }
+  P->u1_elems += lp;
   P->all_tasks.clear();
   for (auto& g : P->groups) P->all_tasks.insert(P->all_tasks.end(), g.tasks.begin(), g.tasks.end());
   return KYM_OK;
@@ -354,6 +370,7 @@ static int make_group(CascadePlan* P, Group& g, int mr, int mc, int kr, int kc, 
   L.sc = sc;
   L.modulus = modulus ? 1 : 0;
   L.src_image = src_image ? 1 : 0;
+  L.bsum_off = -1;
   if (!make_fft_plan(mc, &L.prow, kThreads) || !make_fft_plan(mr, &L.pcol, kThreads) ||
       !make_fft_plan(sc, &L.psrow, kThreads) || !make_fft_plan(sr, &L.pscol, kThreads))
     return KYM_ERR_UNSUPPORTED;
@@ -398,6 +415,7 @@ static int make_group(CascadePlan* P, Group& g, int mr, int mc, int kr, int kc, 
       g.ct = *e;
       g.smem = e->smem;
     }
+    if (!P->oned && L.cluster > 1) g.lines = lines_find(mr, mc, sr, sc, kf);
   }
   L.load_scale = src_image ? 1.f : (float)(1.0 / ((double)kr * kc) / (modulus ? (double)mr * mc : 1.0));
   L.s_scale = (float)(1.0 / ((double)(mr / sr) * (mc / sc)) / ((double)sr * sc));
@@ -544,6 +562,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           cudaEventRecord(e0, stream);
         }
         if (a.lp && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
+        else if (g.lines) err = g.lines(Li, F, ni, stream);
         else if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
         else if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
         else if (Li.cluster > 1) err = launch_group<true, false>(g, Li, F, ni, stream);
@@ -936,7 +955,8 @@ static int run_backward(CascadePlan* P, const float* x, const float* gout, float
         L.dst = u1;
         L.dst_stride = P->u1_elems;
       }
-      if (g.has_ct) err = g.ct.fn(L, F, nimg, stream);
+      if (g.lines) err = g.lines(L, F, nimg, stream);
+      else if (g.has_ct) err = g.ct.fn(L, F, nimg, stream);
       else if (g.oned) err = launch_group<false, true>(g, L, F, nimg, stream);
       else if (L.cluster > 1) err = launch_group<true, false>(g, L, F, nimg, stream);
       else err = launch_group<false, false>(g, L, F, nimg, stream);
@@ -1306,6 +1326,14 @@ extern "C" int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, floa
 extern "C" int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group) {
   if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
   return plan->p.groups[group].has_tc ? 1 : 0;
+}
+
+extern "C" int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores) {
+  if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
+  const kym::Group& g = plan->p.groups[group];
+  if (tensor_cores && g.has_tc) return 1;
+  if (g.lines) return g.L.modulus ? 4 : 3;  // rows, columns, [rows + fold], low-pass
+  return 1;
 }
 
 extern "C" size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch) {

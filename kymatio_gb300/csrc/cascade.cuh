@@ -61,6 +61,7 @@ struct CascadeLaunch {
   const float2* tw_rl;  // exp(-2 pi i k / (mr / cluster)): local column length of a cluster split
   float2* ysave;        // non-null: store y = IFFT2(...) before the modulus (saved for the backward)
   long long ysave_stride;
+  long long bsum_off;   // line-split modulus groups: folded low-pass blocks at dst + img * dst_stride + bsum_off
 };
 
 }  // namespace kym

@@ -32,3 +32,37 @@ const CtEntry* ct_find(int mr, int mc, int sr, int sc, int c, bool oned, int kf)
 }
 
 }  // namespace kym
+
+// ---- line-split variants (lines.cuh) ----------------------------------------
+#include "lines.cuh"
+
+namespace kym {
+
+namespace {
+struct LinesEntry {
+  int mr, mc, sr, sc, kf;
+  LinesLauncher fn;
+};
+std::vector<LinesEntry>& lines_table() {
+  static std::vector<LinesEntry> t;
+  return t;
+}
+}  // namespace
+
+void lines_register(int mr, int mc, int sr, int sc, int kf, LinesLauncher fn) {
+  std::lock_guard<std::mutex> lock(ct_mutex());
+  lines_table().push_back(LinesEntry{mr, mc, sr, sc, kf, fn});
+}
+
+LinesLauncher lines_find(int mr, int mc, int sr, int sc, int kf) {
+  std::lock_guard<std::mutex> lock(ct_mutex());
+  LinesLauncher generic = nullptr;
+  for (const LinesEntry& e : lines_table()) {
+    if (e.mr != mr || e.mc != mc || e.sr != sr || e.sc != sc) continue;
+    if (e.kf == kf) return e.fn;
+    if (e.kf < 0) generic = e.fn;
+  }
+  return generic;
+}
+
+}  // namespace kym
