@@ -297,7 +297,7 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
 }
 
 template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(NT, occupancy_blocks(CtEngine<MR, MC, SR, SC, C, ONED, NT>::smem, NT))
     ct_bwd_kernel(const __grid_constant__ BwdLaunch L, const __grid_constant__ FilterTable F) {
   using E = CtEngine<MR, MC, SR, SC, C, ONED, NT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -31,12 +31,22 @@ __device__ __forceinline__ int ct_reflect(int i, int n) {
   return i < n ? i : period - i;
 }
 
+// CTAs per SM a kernel's register budget is sized for: as many as 200 KB of
+// shared memory holds, keeping at least 64 registers a thread.
+__host__ __device__ constexpr int occupancy_blocks(size_t smem, int nt) {
+  const int by_smem = (int)((size_t)200 * 1024 / (smem ? smem : 1));
+  const int by_regs = 65536 / (nt * 64);
+  const int b = by_smem < by_regs ? by_smem : by_regs;
+  return b < 1 ? 1 : b;
+}
+
 template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
 struct CtGeom {
   static constexpr int RL = MR / C;                                  // rows per CTA
   static constexpr int LD = ONED ? MC + (MC >> 4) + 1 : (MC % 2 == 0 ? MC + 1 : MC);
   static constexpr int LDB = ONED ? SC + (SC >> 4) + 1 : (SC % 2 == 0 ? SC + 1 : SC);
   static constexpr size_t smem = ((size_t)RL * LD + (size_t)SR * LDB) * sizeof(float2);
+  static constexpr int kMinBlocks = occupancy_blocks(smem, NT);
   static_assert(MR % C == 0 && MC % C == 0, "cluster split");
   static_assert(MR % SR == 0 && MC % SC == 0, "low-pass fold");
 };
@@ -191,7 +201,7 @@ __device__ __forceinline__ void ct_cols(float2* A, int rank, const float2* tw, c
 }
 
 template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(NT, (CtGeom<MR, MC, SR, SC, C, ONED, NT>::kMinBlocks))
     ct_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
   using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
   constexpr int RL = G::RL, LD = G::LD, LDB = G::LDB;

@@ -47,7 +47,7 @@ struct TcGeom {
 };
 
 template <int MR, int MC, int NOUTR, int NOUTC, int KF, int NT>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::smem, NT))
     tc_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F,
                       const __grid_constant__ LowpassTable LP, unsigned* status) {
   using G = TcGeom<MR, MC, NOUTC>;
