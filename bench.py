@@ -440,11 +440,15 @@ def run_ours(args, world, rank, local):
         pass
     hbm_peak = peaks.get('hbm_gbs', 6800.0)
     achieved = bytes_launch / dur_s / 1e9
+    # DRAM bytes of one launch of this group, from the committed ncu summary
+    # (null when the dominant group has no capture)
     traffic = None
+    form_key = 'tc' if uses_tc else ('lines' if nkern > 1 else 'fused')
+    tkey = 'L%d_%dx%d_f%d_%s' % (lvl, rows, cols, fold, form_key)
     tf = os.path.join(ROOT, 'profiles', 'dominant_traffic.json')
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf)).get('bytes_per_launch')
+            traffic = json.load(open(tf)).get('kernels', {}).get(tkey, {}).get('bytes_per_launch')
         except Exception:
             traffic = None
     flops_img = fft_flops_per_image()
