@@ -39,6 +39,14 @@ const char* kym_last_error(void);
  * setting. */
 int kym_set_specialized(int enable);
 
+/* In kym_s2d_forward_tc, run the small childless groups that have one
+ * (68x68 at 256x256 J=3) in the DFT-GEMM form: the inverse 2-D DFT and the
+ * low-pass product as split-precision tcgen05 GEMMs (enable=1), or in the
+ * low-pass-only tensor-core form (enable=0, the default).  Takes effect at the
+ * next call.  Returns the previous setting.  No counterpart in the
+ * reference (a form of kymatio/scattering2d/core/scattering2d.py:48-75). */
+int kym_set_tc_dft(int enable);
+
 /* ------------------------------------------------------------------------
  * 2-D scattering (replaces the forward of ScatteringTorch2D,
  * kymatio/scattering2d/frontend/torch_frontend.py:72-111, driving
@@ -96,7 +104,8 @@ int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int
                        int n_filters, const float* const* lowpass_rows, const float* const* lowpass_cols,
                        int n_lowpass, void* workspace, size_t workspace_bytes, unsigned* status, void* stream,
                        float* group_ms, int max_groups);
-/* 1 if launch group `group` runs a tensor-core variant in kym_s2d_forward_tc. */
+/* Tensor-core form of launch group `group` in kym_s2d_forward_tc: 0 none
+ * (FP32 kernel), 1 the low-pass product on tcgen05, 2 the DFT-GEMM form. */
 int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);
 /* Kernel launches that group `group` makes per chunk of images: 1 for a
  * fused cascade kernel, 3 or 4 for the line-split passes of the sizes above

@@ -17,7 +17,7 @@
 #include "cascade.cuh"
 #include "ct_cascade.cuh"
 #include "bwd.cuh"
-#include "tc_cascade.cuh"
+#include "tcdft.cuh"
 #include "lines.cuh"
 #include "plan_util.h"
 #include "errors.h"
@@ -228,6 +228,7 @@ struct Group {
   bool has_tc = false;   // a tensor-core variant exists (childless tasks only)
   size_t tc_smem = 0;
   TcLauncher tc = nullptr;
+  TcLauncher tcdft = nullptr;     // DFT-GEMM tensor-core variant (childless tasks of the small sizes)
   LinesLauncher lines = nullptr;  // line-split passes (sizes above one CTA, every task owns a slot)
   std::vector<Task> tasks;
   size_t task_off = 0;   // offset into the device task array
@@ -238,6 +239,7 @@ struct Group {
 
 int odd_pitch(int n) { return (n % 2 == 0) ? n + 1 : n; }
 std::atomic<bool> g_use_ct{true};
+std::atomic<bool> g_use_tcdft{false};
 int swz_len(int n) { return n + (n >> 4) + 1; }
 
 }  // namespace
@@ -561,7 +563,8 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           cudaEventCreate(&e1);
           cudaEventRecord(e0, stream);
         }
-        if (a.lp && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
+        if (a.lp && g.tcdft && g_use_tcdft.load()) err = g.tcdft(Li, F, *a.lp, a.status, ni, stream);
+        else if (a.lp && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
         else if (g.lines) err = g.lines(Li, F, ni, stream);
         else if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
         else if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
@@ -641,6 +644,8 @@ static void attach_tc(CascadePlan* P) {
       g.has_tc = true;
       g.tc_smem = smem;
       g.tc = fn;
+      if (tcdft_find(g.L.mr, g.L.mc, g.L.out_nr, g.L.out_nc, g.L.kr, &smem, &fn) && smem <= max_dynamic_smem())
+        g.tcdft = fn;
     }
   }
 }
@@ -1245,6 +1250,10 @@ extern "C" int kym_set_specialized(int enable) {
   return kym::g_use_ct.exchange(enable != 0) ? 1 : 0;
 }
 
+extern "C" int kym_set_tc_dft(int enable) {
+  return kym::g_use_tcdft.exchange(enable != 0) ? 1 : 0;
+}
+
 extern "C" int kym_s2d_plan_destroy(kym_s2d_plan* plan) {
   delete plan;
   return KYM_OK;
@@ -1325,7 +1334,9 @@ extern "C" int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, floa
 
 extern "C" int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group) {
   if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
-  return plan->p.groups[group].has_tc ? 1 : 0;
+  const auto& g = plan->p.groups[group];
+  if (g.tcdft && kym::g_use_tcdft.load()) return 2;
+  return g.has_tc ? 1 : 0;
 }
 
 extern "C" int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores) {

@@ -2,7 +2,7 @@
 #include <mutex>
 #include <vector>
 
-#include "tc_cascade.cuh"
+#include "tcdft.cuh"
 
 namespace kym {
 namespace {
@@ -29,6 +29,38 @@ void tc_register(int mr, int mc, int nr, int nc, int kf, size_t smem, TcLauncher
 bool tc_find(int mr, int mc, int nr, int nc, int kf, size_t* smem, TcLauncher* fn) {
   std::lock_guard<std::mutex> lock(mu());
   for (const TcEntry& e : table())
+    if (e.mr == mr && e.mc == mc && e.nr == nr && e.nc == nc && e.kf == kf) {
+      *smem = e.smem;
+      *fn = e.fn;
+      return true;
+    }
+  return false;
+}
+
+}  // namespace kym
+
+namespace kym {
+namespace {
+struct TcEntryList {
+  std::vector<TcEntry> v;
+  std::mutex mu;
+};
+TcEntryList& dft_table() {
+  static TcEntryList t;
+  return t;
+}
+}  // namespace
+
+void tcdft_register(int mr, int mc, int nr, int nc, int kf, size_t smem, TcLauncher fn) {
+  TcEntryList& t = dft_table();
+  std::lock_guard<std::mutex> lock(t.mu);
+  t.v.push_back(TcEntry{mr, mc, nr, nc, kf, smem, fn});
+}
+
+bool tcdft_find(int mr, int mc, int nr, int nc, int kf, size_t* smem, TcLauncher* fn) {
+  TcEntryList& t = dft_table();
+  std::lock_guard<std::mutex> lock(t.mu);
+  for (const TcEntry& e : t.v)
     if (e.mr == mr && e.mc == mc && e.nr == nr && e.nc == nc && e.kf == kf) {
       *smem = e.smem;
       *fn = e.fn;

@@ -49,9 +49,42 @@ def test_tc_form_vs_fp64_oracle(J, side, B):
     plan = S._get_plan()
     lib = _lib.load()
     used = [lib.kym_s2d_group_uses_tc(plan.h, g) for g in range(lib.kym_s2d_group_count(plan.h))]
-    assert any(u == 1 for u in used), used
+    assert any(u >= 1 for u in used), used
     out = S(torch.from_numpy(x).to(dev)).cpu().numpy()
     assert S.tensor_core_status() == 0
     for k, sl in enumerate(order_slices(J, 8, 2)):
         e = rel_l2(out[:, sl], ref[:, sl])
         assert e <= TOL_TC, 'order %d relL2 %.3e' % (k, e)
+
+
+def test_dft_gemm_form_256_J3():
+    """The 68x68 childless groups of 256x256 J=3 in the DFT-GEMM form (inverse
+    DFT and low-pass as split-precision tcgen05 GEMMs): per-order relative L2
+    against the FP64 oracle, and against the low-pass-only tensor-core form.
+    Three images give 192 tasks per order-2 group, more than one per CTA of
+    the persistent grid."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from kymatio_gb300 import Scattering2D, _lib
+    from oracle.scattering2d import Scattering2D as Oracle, order_slices
+    lib = _lib.load()
+    dev = torch.device('cuda:0')
+    x = np.random.default_rng(68).random((3, 256, 256)).astype(np.float32)
+    S = Scattering2D(3, (256, 256), backend='torch_tc').to(dev)
+    plan = S._get_plan()
+    xd = torch.from_numpy(x).to(dev)
+    prev = lib.kym_set_tc_dft(1)
+    try:
+        used = [lib.kym_s2d_group_uses_tc(plan.h, g) for g in range(lib.kym_s2d_group_count(plan.h))]
+        assert used.count(2) == 3, used
+        out_dft = S(xd).cpu().numpy()
+        assert S.tensor_core_status() == 0
+        lib.kym_set_tc_dft(0)
+        out_lp = S(xd).cpu().numpy()
+    finally:
+        lib.kym_set_tc_dft(prev)
+    ref = Oracle(3, (256, 256))(x.astype(np.float64))
+    for k, sl in enumerate(order_slices(3, 8, 2)):
+        e = rel_l2(out_dft[:, sl], ref[:, sl])
+        assert e <= TOL_TC, 'order %d relL2 %.3e' % (k, e)
+        assert rel_l2(out_dft[:, sl], out_lp[:, sl]) <= TOL_TC
