@@ -273,6 +273,7 @@ struct CascadePlan {
   std::vector<int> filter_rows, filter_cols;  // expected filter shapes, by index
   long long u0_elems = 0;                     // per image
   long long u1_elems = 0;                     // per image
+  size_t opnd_bytes = 0;                      // per image: DFT-GEMM operand slots of the largest such group
   int chunk = 0;
   std::vector<Group> groups;
   std::vector<Task> all_tasks;
@@ -470,6 +471,7 @@ struct RunArgs {
   float* group_ms = nullptr;
   int max_groups = 0;
   float2* ysave = nullptr;  // non-null: every path stores its modulus input (per image gy2 + gy1 elements)
+  unsigned char* opnd = nullptr;  // DFT-GEMM operand slots (chunk images)
 };
 
 static int fail_cuda(cudaError_t e, const char* what) {
@@ -523,6 +525,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
       L.tw_rl = L.cluster > 1 ? ds->tw + P->tw.offset(L.mr / L.cluster) : nullptr;
       L.x = x;
       L.x_stride = x_stride;
+      L.opnd = a.opnd;
       L.out = out;
       L.out_stride = out_stride;
       if (a.ysave && g.level > 0) {
@@ -563,7 +566,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           cudaEventCreate(&e1);
           cudaEventRecord(e0, stream);
         }
-        if (a.lp && g.tcdft && g_use_tcdft.load()) err = g.tcdft(Li, F, *a.lp, a.status, ni, stream);
+        if (a.lp && g.tcdft && a.opnd) err = g.tcdft(Li, F, *a.lp, a.status, ni, stream);
         else if (a.lp && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
         else if (g.lines) err = g.lines(Li, F, ni, stream);
         else if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
@@ -610,7 +613,14 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   int rc = make_filter_table(P, filters, nfilters, &F);
   if (rc) return rc;
   const int chunk = std::min(batch, P->chunk);
-  const size_t need = ((size_t)batch * P->u0_elems + (size_t)chunk * P->u1_elems) * sizeof(float2);
+  const size_t spectra = ((size_t)batch * P->u0_elems + (size_t)chunk * P->u1_elems) * sizeof(float2);
+  // the DFT-GEMM groups of the tensor-core form keep their operand slots after the spectra
+  const size_t opnd_off = (spectra + 255) & ~(size_t)255;
+  // the fold pass copies source and wavelet rows with TMA: 16-byte-aligned bases
+  bool aligned = (reinterpret_cast<uintptr_t>(workspace) & 15) == 0;
+  for (int i = 0; aligned && i < nfilters; ++i) aligned = (reinterpret_cast<uintptr_t>(filters[i]) & 15) == 0;
+  const bool dft = lp && !ysave && P->opnd_bytes && g_use_tcdft.load() && aligned;
+  const size_t need = dft ? opnd_off + (size_t)chunk * P->opnd_bytes : spectra;
   if (!workspace || ws_bytes < need) {
     set_error_message("forward", "workspace missing or smaller than the plan requires");
     return KYM_ERR_WORKSPACE;
@@ -627,6 +637,7 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   a.lp = ysave ? nullptr : lp;  // the tensor-core kernels do not save y
   a.status = status;
   a.ysave = ysave;
+  if (dft) a.opnd = static_cast<unsigned char*>(workspace) + opnd_off;
   return run_core(P, x, out, batch, F, a, stream);
 }
 
@@ -644,8 +655,21 @@ static void attach_tc(CascadePlan* P) {
       g.has_tc = true;
       g.tc_smem = smem;
       g.tc = fn;
-      if (tcdft_find(g.L.mr, g.L.mc, g.L.out_nr, g.L.out_nc, g.L.kr, &smem, &fn) && smem <= max_dynamic_smem())
+      // the DFT-GEMM fold pass reads its paths as a P x 8 grid: path p * 8 + q
+      // folds source p with wavelet q (sources and wavelets shared along rows
+      // and columns), from 16-byte-aligned rows
+      bool grid = (g.tasks.size() == 8 || g.tasks.size() == 64) && (P->u0_elems % 2 == 0);
+      for (size_t i = 0; grid && i < g.tasks.size(); ++i) {
+        const Task& t = g.tasks[i];
+        grid = t.src_off % 2 == 0 && t.src_off == g.tasks[i / 8 * 8].src_off && t.psi == g.tasks[i % 8].psi &&
+               t.phi == g.tasks[0].phi;
+      }
+      if (grid && tcdft_find(g.L.mr, g.L.mc, g.L.out_nr, g.L.out_nc, g.L.kr, &smem, &fn) &&
+          smem <= max_dynamic_smem()) {
         g.tcdft = fn;
+        const size_t mp = (size_t)(g.L.mr + 7) / 8 * 8;
+        P->opnd_bytes = std::max(P->opnd_bytes, g.tasks.size() * 8 * mp * mp);
+      }
     }
   }
 }
@@ -1351,7 +1375,9 @@ extern "C" size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch) {
   if (!plan || batch < 0) return 0;
   const CascadePlan& P = plan->p;
   const int chunk = std::min(batch, P.chunk);
-  return ((size_t)batch * P.u0_elems + (size_t)chunk * P.u1_elems) * sizeof(float2);
+  const size_t spectra = ((size_t)batch * P.u0_elems + (size_t)chunk * P.u1_elems) * sizeof(float2);
+  if (!P.opnd_bytes) return spectra;
+  return ((spectra + 255) & ~(size_t)255) + (size_t)chunk * P.opnd_bytes;
 }
 
 namespace kym {

@@ -62,6 +62,7 @@ struct CascadeLaunch {
   float2* ysave;        // non-null: store y = IFFT2(...) before the modulus (saved for the backward)
   long long ysave_stride;
   long long bsum_off;   // line-split modulus groups: folded low-pass blocks at dst + img * dst_stride + bsum_off
+  unsigned char* opnd;  // DFT-GEMM form: per-path operand slots of the launch (image-major, then task)
 };
 
 }  // namespace kym

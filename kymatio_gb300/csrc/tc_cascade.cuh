@@ -78,6 +78,31 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
   }
   if (tid == 0) tc::mbar_init(mbar, 1);
 
+  // Operand B first: its loads from the low-pass table overlap the fold
+  // below (its region is disjoint from the FFT array).
+  constexpr int G8 = KP / 8;  // 16-byte chunks per operand row
+  // B = T_c (NP x KP, rows beyond NOUTC and columns beyond MC zero)
+  const float* tcm = LP.c[t.phi];
+  const size_t b_half = (size_t)NP * KP * 2;
+  for (int g = tid; g < NP * G8; g += NT) {
+    const int r = g % NP, c = g / NP;
+    uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
+    if (r < NOUTC) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = 8 * c + q;
+        const float v = k < MC ? __ldg(tcm + r * MC + k) : 0.f;
+        __nv_bfloat16 bh, bl;
+        tc::split_bf16(v, bh, bl);
+        h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
+        l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
+      }
+    }
+    const uint32_t off = tc::kmajor_offset(r, 8 * c, KP);
+    *reinterpret_cast<uint4*>(bop + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(bop + b_half + off) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+
   // ---- U = |IFFT2(fold(src * psi))| -----------------------------------------
   ct_load<MR, MC, 1, false, NT, KF, LD>(A, L, F, t, img, 0);
   __syncthreads();
@@ -88,7 +113,6 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
   // consecutive items are the 8 rows of one core matrix (128 contiguous
   // bytes).  Rows beyond MR are never written: they only feed output rows
   // that are discarded.  Columns beyond MC are zero.
-  constexpr int G8 = KP / 8;              // chunks per row
   constexpr int MR8 = (MR + 7) / 8 * 8;   // rows rounded to whole core matrices
   constexpr int NIT = MR8 * G8;
   constexpr int PER = (NIT + NT - 1) / NT;
@@ -134,27 +158,6 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
       *reinterpret_cast<uint4*>(aop + a_half + off) = lo4[i];
     }
   }
-  // operand B = T_c (NP x KP, rows beyond NOUTC and columns beyond MC zero)
-  const float* tcm = LP.c[t.phi];
-  const size_t b_half = (size_t)NP * KP * 2;
-  for (int g = tid; g < NP * G8; g += NT) {
-    const int r = g % NP, c = g / NP;
-    uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
-    if (r < NOUTC) {
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int k = 8 * c + q;
-        const float v = k < MC ? __ldg(tcm + r * MC + k) : 0.f;
-        __nv_bfloat16 bh, bl;
-        tc::split_bf16(v, bh, bl);
-        h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
-        l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
-      }
-    }
-    const uint32_t off = tc::kmajor_offset(r, 8 * c, KP);
-    *reinterpret_cast<uint4*>(bop + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4*>(bop + b_half + off) = make_uint4(l[0], l[1], l[2], l[3]);
-  }
   tc::fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
@@ -181,6 +184,15 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
     }
     tc::mma_commit(mbar);
   }
+  // T_r (NOUTR x MR) is read by every output below: fetched into registers
+  // while the tensor cores run, staged in the operand-A region once they finish
+  constexpr int TRN = NOUTR * MR;
+  constexpr int TRP = (TRN + NT - 1) / NT;
+  static_assert((size_t)TRN * sizeof(float) <= G::region0, "T_r staging overlaps the product tile");
+  const float* trm = LP.r[t.phi];
+  float trv[TRP];
+#pragma unroll
+  for (int i = 0; i < TRP; ++i) trv[i] = (tid + i * NT < TRN) ? __ldg(trm + tid + i * NT) : 0.f;
   bool ok = tc::mbar_wait_bounded(mbar, 0, 1u << 24);
   if (!ok) {
     if (tid == 0) atomicOr(status, tc::kErrMmaTimeout);
@@ -203,21 +215,24 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
       }
     }
   }
+  float* trs = reinterpret_cast<float*>(smem);  // the operand-A region: the MMA has finished reading it
+#pragma unroll
+  for (int i = 0; i < TRP; ++i)
+    if (tid + i * NT < TRN) trs[tid + i * NT] = trv[i];
   tc::fence_before_sync();
   __syncthreads();
   if (tid < 32) tc::tmem_dealloc(taddr, G::TMEM_COLS);
 
   // ---- S = T_r * T on the FP32 pipe, written to the output channel -----------------
-  const float* trm = LP.r[t.phi];
   float* out = L.out + (size_t)(L.img0 + img) * L.out_stride + (size_t)t.out_ch * NOUTR * NOUTC;
   for (int o = tid; o < NOUTR * NOUTC; o += NT) {
     const int p = o / NOUTC, q = o % NOUTC;
-    const float* tr = trm + p * MR;
+    const float* tr = trs + p * MR;
     float acc0 = 0.f, acc1 = 0.f;
 #pragma unroll 4
     for (int x = 0; x < MR; x += 2) {
-      acc0 = fmaf(__ldg(tr + x), T[x * TLD + q], acc0);
-      if (x + 1 < MR) acc1 = fmaf(__ldg(tr + x + 1), T[(x + 1) * TLD + q], acc1);
+      acc0 = fmaf(tr[x], T[x * TLD + q], acc0);
+      if (x + 1 < MR) acc1 = fmaf(tr[x + 1], T[(x + 1) * TLD + q], acc1);
     }
     out[o] = ok ? acc0 + acc1 : __int_as_float(0x7fc00000);
   }

@@ -15,19 +15,25 @@
 //   then    S[p][q] = sum_y T_c[q][y] T'[y][p]      (FP32 pipe)
 // Wop = [[Re W, -Im W], [Im W, Re W]] is built once on the host in FP64,
 // split into BF16 hi + lo, laid out as the shared-memory operand image and
-// copied into shared memory with one TMA bulk copy per CTA; it stays resident
-// while the CTA walks its tasks (persistent grid, one CTA per SM).  Every
-// operand x enters as hi = bf16(x), lo = bf16(x - hi) and each GEMM sums
+// copied into shared memory with TMA bulk copies; it stays resident while the
+// CTA walks its paths (persistent grid, one CTA per SM).  Every operand x
+// enters as hi = bf16(x), lo = bf16(x - hi) and each GEMM sums
 // A_hi B_hi + A_lo B_hi + A_hi B_lo.
 //
-// Shared memory (bytes, MP = M rounded up to 8; SBO = 32 MP):
-//   [0, 4 MP^2)        operand A / Z^T, hi half (rows 0..MP-1)
-//   [4 MP^2, 8 MP^2)   operand A / Z^T, lo half
-//   [8 MP^2, 24 MP^2)  Wop hi | lo (2 MP rows each), resident
-//   [24 MP^2, +32)     mbarriers, TMEM base
+// The fold (the streaming read of the source spectrum and the wavelet) runs
+// as a separate high-occupancy pass that writes each path's step-1 operand
+// image to a slot in global memory; the GEMM kernel copies path k+1's image
+// into its second buffer (TMA bulk copy) while path k is computed.
+//
+// Shared memory (bytes, MP = M rounded up to 8; SBO = 32 MP; slot = 8 MP^2):
+//   [0, slot)             buffer 0: operand A / Z^T (hi rows, lo rows), then
+//                         the step-3 operand and T'
+//   [slot, 2 slot)        buffer 1
+//   [2 slot, +16 MP^2)    Wop hi | lo (2 MP rows each), resident
+//   then                  T_r as the step-3 B operand (hi | lo) and T_c (fp32),
+//                         resident per low-pass filter; mbarriers, TMEM base
 // The M = 128 tile reads rows MP..127 past each half: those rows hold other
-// data and only produce accumulator rows that are never read.  Steps 3 and
-// the T' read-back reuse [0, 8 MP^2).
+// data and only produce accumulator rows that are never read.
 #pragma once
 #include "tc_cascade.cuh"
 
@@ -40,27 +46,36 @@ struct DftGeom {
   static constexpr int NP = 2 * MP;  // N: [Re | Im] halves of the output
   static constexpr uint32_t SBO = (uint32_t)(KP / 8) * 128u;
   static constexpr size_t half_a = (size_t)(MP / 8) * SBO;
-  static constexpr size_t off_ah = 0, off_al = half_a;
+  // one path's step-1 operand (hi rows, then lo rows): the unit the fold pass
+  // writes to global memory and the kernel copies into one of two buffers
+  static constexpr uint32_t slot_bytes = (uint32_t)(2 * half_a);
   static constexpr size_t w_half = (size_t)(NP / 8) * SBO;
-  static constexpr size_t off_wh = 2 * half_a, off_wl = off_wh + w_half;
+  static constexpr size_t off_wh = 2 * (size_t)slot_bytes, off_wl = off_wh + w_half;
   static constexpr int K3 = (M + 15) / 16 * 16;
   static constexpr int N3 = NOUT < 16 ? 16 : (NOUT + 15) / 16 * 16;
   static constexpr uint32_t SBO3 = (uint32_t)(K3 / 8) * 128u;
   static constexpr size_t half_a3 = (size_t)(MP / 8) * SBO3;
   static constexpr size_t half_b3 = (size_t)(N3 / 8) * SBO3;
-  static constexpr size_t off_a3h = 0, off_a3l = half_a3, off_b3h = 2 * half_a3, off_b3l = off_b3h + half_b3;
+  static constexpr size_t off_a3l = half_a3;  // within the path's buffer
   static constexpr int TLD = N3 + 1;  // fp32 pitch of T'
-  static constexpr size_t bar_off = off_wl + w_half;
-  static constexpr size_t smem = bar_off + 32;
+  // resident low-pass factors of the group: T_r as the step-3 B operand, T_c in fp32
+  static constexpr size_t off_b3h = off_wl + w_half, off_b3l = off_b3h + half_b3;
+  static constexpr size_t off_tc = off_b3l + half_b3;
+  static constexpr int TCLD = M + 1;  // fp32 pitch of T_c (conflict-free column reads)
+  static constexpr int MAX_TASKS = 64;
+  static constexpr size_t off_tasks = (off_tc + (size_t)NOUT * TCLD * 4 + 15) / 16 * 16;
+  static constexpr size_t bar_off = off_tasks + (size_t)MAX_TASKS * sizeof(Task);
+  static constexpr size_t smem = bar_off + 48;  // wbar, mbar, full[2], TMEM base
   static constexpr int C3 = (NP + 31) / 32 * 32;  // TMEM column of D3
   static constexpr int TMEM_COLS = 256;
   static constexpr uint32_t w_bytes = (uint32_t)(2 * w_half);
   static_assert(M % 4 == 0 && M <= 120, "work size");
   static_assert(NP <= 256 && C3 + N3 <= TMEM_COLS, "accumulator tile too wide");
-  static_assert(off_b3l + half_b3 <= off_wh, "low-pass operands overlap the resident DFT matrix");
-  static_assert((size_t)M * TLD * 4 <= off_wh, "T' overlaps the resident DFT matrix");
-  static_assert(off_al + 16 * (size_t)SBO <= smem && off_a3l + 16 * (size_t)SBO3 <= smem,
-                "M-tile reads stay inside the allocation");
+  static_assert(2 * half_a3 <= slot_bytes && (size_t)M * TLD * 4 <= slot_bytes,
+                "step-3 operand and T' fit the path's buffer");
+  static_assert(slot_bytes % 16 == 0, "TMA bulk copies move multiples of 16 bytes");
+  static_assert(slot_bytes + half_a + 16 * (size_t)SBO <= smem && slot_bytes + off_a3l + 16 * (size_t)SBO3 <= smem,
+                "M-tile reads of the second buffer stay inside the allocation");
 };
 
 namespace dft {
@@ -90,6 +105,14 @@ __device__ __forceinline__ void store_one(unsigned char* hi, unsigned char* lo, 
   *reinterpret_cast<__nv_bfloat16*>(lo + off) = l;
 }
 
+// Hardware square root (sqrt.approx.f32, relative error about 2^-23): the
+// modulus feeds a BF16 hi/lo split, far coarser than its rounding.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // D (+)= A B^T over ksteps K-steps of 16, three split products per step.
 __device__ __forceinline__ void split_gemm(uint32_t d, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl,
                                            uint32_t sbo, uint32_t idesc, int ksteps) {
@@ -116,75 +139,170 @@ __device__ __forceinline__ bool cta_wait(uint64_t* bar, uint32_t parity, unsigne
   return true;
 }
 
-// A = fold_KF(src * psi) * load_scale, written as the step-1 operand:
-// row u, K chunk c (columns 8c..8c+7) for Re and chunk MP/8 + c for Im.
-template <int M, int KF, int NT, int MP>
-__device__ __forceinline__ void load_fold(unsigned char* ah, unsigned char* al, const CascadeLaunch& L,
-                                          const FilterTable& F, const Task& t, int img) {
-  constexpr int NCH = MP / 8, SCOLS = KF * M, KP = 2 * MP;
+// One 8-column chunk of A = fold_KF(src * psi) * load_scale: row u,
+// columns 8c..8c+7 (columns at or beyond M are zero).
+template <int M, int KF>
+__device__ __forceinline__ void fold_chunk(const CascadeLaunch& L, const FilterTable& F, const Task& t, int img,
+                                           int u, int c, float (&re)[8], float (&im)[8]) {
+  constexpr int SCOLS = KF * M;
   const float4* src4 = reinterpret_cast<const float4*>(L.src + (size_t)img * L.src_stride + t.src_off);
   const float2* psi2 = reinterpret_cast<const float2*>(F.f[t.psi]);
-  const float sc = L.load_scale;
-  for (int e = threadIdx.x; e < M * NCH; e += NT) {
-    const int u = e / NCH, c = e % NCH;
-    const int v0 = 8 * c;
-    const bool full = v0 + 8 <= M;  // M % 8 == 4: the last chunk holds 4 columns
-    float re[8], im[8];
+  const int v0 = 8 * c;
+  const bool full = v0 + 8 <= M;  // M % 8 == 4: the last chunk holds 4 columns
 #pragma unroll
-    for (int i = 0; i < 8; ++i) re[i] = im[i] = 0.f;
+  for (int i = 0; i < 8; ++i) re[i] = im[i] = 0.f;
 #pragma unroll
-    for (int a = 0; a < KF; ++a) {
+  for (int a = 0; a < KF; ++a) {
 #pragma unroll
-      for (int b = 0; b < KF; ++b) {
-        const size_t base = (size_t)(u + a * M) * SCOLS + v0 + b * M;  // a multiple of 4
-        const float4* s = src4 + (base >> 1);
-        const float2* f = psi2 + (base >> 1);
-        const float4 s0 = __ldg(s), s1 = __ldg(s + 1);
-        const float2 f0 = __ldg(f), f1 = __ldg(f + 1);
-        re[0] = fmaf(s0.x, f0.x, re[0]); im[0] = fmaf(s0.y, f0.x, im[0]);
-        re[1] = fmaf(s0.z, f0.y, re[1]); im[1] = fmaf(s0.w, f0.y, im[1]);
-        re[2] = fmaf(s1.x, f1.x, re[2]); im[2] = fmaf(s1.y, f1.x, im[2]);
-        re[3] = fmaf(s1.z, f1.y, re[3]); im[3] = fmaf(s1.w, f1.y, im[3]);
-        if (full) {
-          const float4 s2 = __ldg(s + 2), s3 = __ldg(s + 3);
-          const float2 f2 = __ldg(f + 2), f3 = __ldg(f + 3);
-          re[4] = fmaf(s2.x, f2.x, re[4]); im[4] = fmaf(s2.y, f2.x, im[4]);
-          re[5] = fmaf(s2.z, f2.y, re[5]); im[5] = fmaf(s2.w, f2.y, im[5]);
-          re[6] = fmaf(s3.x, f3.x, re[6]); im[6] = fmaf(s3.y, f3.x, im[6]);
-          re[7] = fmaf(s3.z, f3.y, re[7]); im[7] = fmaf(s3.w, f3.y, im[7]);
-        }
+    for (int b = 0; b < KF; ++b) {
+      const size_t base = (size_t)(u + a * M) * SCOLS + v0 + b * M;  // a multiple of 4
+      const float4* s = src4 + (base >> 1);
+      const float2* f = psi2 + (base >> 1);
+      const float4 s0 = __ldg(s), s1 = __ldg(s + 1);
+      const float2 f0 = __ldg(f), f1 = __ldg(f + 1);
+      re[0] = fmaf(s0.x, f0.x, re[0]); im[0] = fmaf(s0.y, f0.x, im[0]);
+      re[1] = fmaf(s0.z, f0.y, re[1]); im[1] = fmaf(s0.w, f0.y, im[1]);
+      re[2] = fmaf(s1.x, f1.x, re[2]); im[2] = fmaf(s1.y, f1.x, im[2]);
+      re[3] = fmaf(s1.z, f1.y, re[3]); im[3] = fmaf(s1.w, f1.y, im[3]);
+      if (full) {
+        const float4 s2 = __ldg(s + 2), s3 = __ldg(s + 3);
+        const float2 f2 = __ldg(f + 2), f3 = __ldg(f + 3);
+        re[4] = fmaf(s2.x, f2.x, re[4]); im[4] = fmaf(s2.y, f2.x, im[4]);
+        re[5] = fmaf(s2.z, f2.y, re[5]); im[5] = fmaf(s2.w, f2.y, im[5]);
+        re[6] = fmaf(s3.x, f3.x, re[6]); im[6] = fmaf(s3.y, f3.x, im[6]);
+        re[7] = fmaf(s3.z, f3.y, re[7]); im[7] = fmaf(s3.w, f3.y, im[7]);
       }
     }
+  }
+  const float sc = L.load_scale;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      re[i] *= sc;
-      im[i] *= sc;
-    }
-    store_chunk(ah, al, u, v0, KP, re);
-    store_chunk(ah, al, u, MP + v0, KP, im);
+  for (int i = 0; i < 8; ++i) {
+    re[i] *= sc;
+    im[i] *= sc;
   }
 }
 
 }  // namespace dft
 
+// Fold pass: A = fold_KF(src * psi) * load_scale for every path of the
+// launch, written as each path's step-1 operand image (hi rows, lo rows;
+// rows M..MP-1 are not written and only feed discarded accumulator rows).
+// The paths form a P x Q grid: path p Q + q folds parent spectrum p (at
+// tasks[p Q].src_off) with wavelet q (tasks[q].psi).  One CTA computes row u
+// of every path of one image, so each source row and wavelet row it needs is
+// read once (TMA bulk copies into shared memory) for all the paths sharing it.
+template <int M, int KF, int P, int Q>
+struct StripGeom {
+  static constexpr int SC = KF * M;                      // source columns
+  static constexpr uint32_t prow = (uint32_t)SC * 8u;     // bytes of one parent row
+  static constexpr uint32_t frow = (uint32_t)SC * 4u;     // bytes of one wavelet row
+  static constexpr uint32_t stage = P * prow + Q * frow;  // rows for one alias a
+  static constexpr uint32_t tx = KF * stage;
+  static constexpr size_t outs = (size_t)P * Q * M * 8;  // the outputs reuse the staging area
+  static constexpr size_t bar_off = ((tx > outs ? (size_t)tx : outs) + 15) / 16 * 16;
+  static constexpr size_t smem = bar_off + 16;
+  static constexpr int NT = (M * P + 31) / 32 * 32;
+  static_assert(prow % 16 == 0 && frow % 16 == 0, "bulk copies of whole 16-byte units");
+};
+
+template <int M, int KF, int P, int Q>
+__global__ void __launch_bounds__(StripGeom<M, KF, P, Q>::NT)
+    tcdft_fold_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F,
+                      unsigned* status) {
+  using G = DftGeom<M, 8>;
+  using S = StripGeom<M, KF, P, Q>;
+  constexpr int MP = G::MP, NCH = MP / 8, KP = G::KP, SC = S::SC, NT = S::NT;
+  extern __shared__ __align__(16) unsigned char sm[];
+  const float2* prow = reinterpret_cast<const float2*>(sm);               // [KF][P][SC]
+  const float* frow = reinterpret_cast<const float*>(sm + KF * P * S::prow);  // [KF][Q][SC]
+  float2* outs = reinterpret_cast<float2*>(sm);                           // [P Q][M], after the fold
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::bar_off);
+  const int u = blockIdx.x, img = blockIdx.y, tid = threadIdx.x;
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0) tc::mbar_expect_tx(bar, S::tx);
+  __syncthreads();  // the expected byte count is set before any copy can complete
+  if (tid < KF * (P + Q)) {
+    // one row copy per thread: alias a, then parent p or wavelet q
+    const int a = tid / (P + Q), w = tid - a * (P + Q);
+    const size_t r = (size_t)(u + a * M) * SC;
+    if (w < P)
+      tc::bulk_g2s(sm + (size_t)(a * P + w) * S::prow,
+                   L.src + (size_t)img * L.src_stride + L.tasks[w * Q].src_off + r, S::prow, bar);
+    else
+      tc::bulk_g2s(sm + (size_t)KF * P * S::prow + (size_t)(a * Q + (w - P)) * S::frow,
+                   F.f[L.tasks[w - P].psi] + r, S::frow, bar);
+  }
+  bool ok = tc::mbar_wait_bounded(bar, 0, 1u << 22);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) atomicOr(status, tc::kErrMmaTimeout);
+    tc::mbar_wait_bounded(bar, 0, 1u << 22);
+    __syncthreads();
+  }
+  // thread (p, v): the Q paths of parent p at column v
+  float2 acc[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) acc[q] = make_float2(0.f, 0.f);
+  const int p = tid / M, v = tid - (tid / M) * M;
+  if (tid < M * P) {
+#pragma unroll
+    for (int a = 0; a < KF; ++a)
+#pragma unroll
+      for (int b = 0; b < KF; ++b) {
+        const float2 sv = prow[(a * P + p) * SC + v + b * M];
+        const float* fr = frow + (size_t)a * Q * SC + v + b * M;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const float f = fr[q * SC];
+          acc[q].x = fmaf(sv.x, f, acc[q].x);
+          acc[q].y = fmaf(sv.y, f, acc[q].y);
+        }
+      }
+  }
+  __syncthreads();  // the staging area now holds the outputs
+  const float sc = ok ? L.load_scale : __int_as_float(0x7fc00000);
+  if (tid < M * P)
+#pragma unroll
+    for (int q = 0; q < Q; ++q) outs[(p * Q + q) * M + v] = make_float2(acc[q].x * sc, acc[q].y * sc);
+  __syncthreads();
+  // row u of every path's operand: 16-byte chunks (hi and lo) of [Re | Im]
+  for (int e = tid; e < P * Q * 2 * NCH; e += NT) {
+    const int t = e / (2 * NCH), r = e - t * (2 * NCH);
+    const int part = r / NCH, c = r - part * NCH;
+    float v8[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int x = 8 * c + i;
+      const float2 z = x < M ? outs[t * M + x] : make_float2(0.f, 0.f);
+      v8[i] = part ? z.y : z.x;
+    }
+    unsigned char* slot = L.opnd + ((size_t)img * L.ntasks + t) * G::slot_bytes;
+    dft::store_chunk(slot, slot + G::half_a, u, part * MP + 8 * c, KP, v8);
+  }
+}
+
+// The GEMM kernel: persistent, one CTA per SM.  Path k of the CTA arrives in
+// buffer k & 1 by TMA bulk copy, issued while path k - 1 is computed.
 template <int M, int NOUT, int KF, int NT>
 __global__ void __launch_bounds__(NT, 1)
-    tcdft_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F,
-                         const __grid_constant__ LowpassTable LP, const unsigned char* __restrict__ wimg, int nimg,
-                         unsigned* status) {
+    tcdft_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ LowpassTable LP,
+                         const unsigned char* __restrict__ wimg, int nimg, unsigned* status) {
   using G = DftGeom<M, NOUT>;
   constexpr int MP = G::MP, KP = G::KP, NP = G::NP, K3 = G::K3, N3 = G::N3, TLD = G::TLD;
   constexpr int NCH = MP / 8;        // 8-column chunks of one [Re | Im] half
   constexpr int WPQ = NT / 128;      // warps per TMEM lane quarter
   static_assert(NT % 128 == 0, "whole lane quarters");
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* ah = smem + G::off_ah;
-  unsigned char* al = smem + G::off_al;
   uint64_t* wbar = reinterpret_cast<uint64_t*>(smem + G::bar_off);
   uint64_t* mbar = wbar + 1;
-  uint32_t* slot = reinterpret_cast<uint32_t*>(smem + G::bar_off + 16);
+  uint64_t* full = wbar + 2;  // full[0], full[1]
+  uint32_t* slot = reinterpret_cast<uint32_t*>(smem + G::bar_off + 32);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3, cgroup = warp >> 2;
+  const int total = L.ntasks * nimg;
 
   if (tid < 32) {
     tc::tmem_alloc(slot, G::TMEM_COLS);
@@ -193,6 +311,8 @@ __global__ void __launch_bounds__(NT, 1)
   if (tid == 0) {
     tc::mbar_init(wbar, 1);
     tc::mbar_init(mbar, 1);
+    tc::mbar_init(&full[0], 1);
+    tc::mbar_init(&full[1], 1);
     tc::mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -200,35 +320,84 @@ __global__ void __launch_bounds__(NT, 1)
   tc::fence_after_sync();
   const uint32_t taddr = *slot;
   if (tid == 0) {
-    // the resident DFT matrix: one TMA bulk copy, in 16 KB pieces
+    // the resident DFT matrix, then the first path's operand
     tc::mbar_expect_tx(wbar, G::w_bytes);
     for (uint32_t o = 0; o < G::w_bytes; o += 16384u)
       tc::bulk_g2s(smem + G::off_wh + o, wimg + o, (G::w_bytes - o) < 16384u ? (G::w_bytes - o) : 16384u, wbar);
+    if ((int)blockIdx.x < total) {
+      tc::mbar_expect_tx(&full[0], G::slot_bytes);
+      tc::bulk_g2s(smem, L.opnd + (size_t)blockIdx.x * G::slot_bytes, G::slot_bytes, &full[0]);
+    }
   }
-  const uint32_t s_ah = tc::smem_addr(ah), s_al = tc::smem_addr(al);
   const uint32_t s_wh = tc::smem_addr(smem + G::off_wh), s_wl = tc::smem_addr(smem + G::off_wl);
-  const uint32_t s_a3h = tc::smem_addr(smem + G::off_a3h), s_a3l = tc::smem_addr(smem + G::off_a3l);
   const uint32_t s_b3h = tc::smem_addr(smem + G::off_b3h), s_b3l = tc::smem_addr(smem + G::off_b3l);
   constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, NP);
   constexpr uint32_t idesc3 = tc::idesc_bf16_f32(128, N3);
-  float* Tp = reinterpret_cast<float*>(smem);
+  float* tcs = reinterpret_cast<float*>(smem + G::off_tc);
+  Task* tasks = reinterpret_cast<Task*>(smem + G::off_tasks);
+  for (int i = tid; i < L.ntasks; i += NT) tasks[i] = L.tasks[i];
+  __syncthreads();
 
-  const int total = L.ntasks * nimg;
   uint32_t ph = 0;
+  int cur_phi = -1;
+  int pending = (int)blockIdx.x < total ? 1 : 0;  // operand copies issued and not yet waited for
   bool alive = dft::cta_wait(wbar, 0, status);
-  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+  int k = 0;
+  for (int item = blockIdx.x; item < total; item += gridDim.x, ++k) {
+    const int b = k & 1;
+    unsigned char* buf = smem + (size_t)b * G::slot_bytes;
+    unsigned char* ah = buf;
+    unsigned char* al = buf + G::half_a;
+    const uint32_t s_ah = tc::smem_addr(ah), s_al = tc::smem_addr(al);
+    const uint32_t s_a3h = s_ah, s_a3l = s_ah + (uint32_t)G::off_a3l;
+    float* Tp = reinterpret_cast<float*>(buf);
     const int img = item / L.ntasks;
-    const Task t = L.tasks[item - img * L.ntasks];
+    const Task t = tasks[item - img * L.ntasks];
     float* out = L.out + (size_t)(L.img0 + img) * L.out_stride + (size_t)t.out_ch * NOUT * NOUT;
     if (!alive) {
       for (int o = tid; o < NOUT * NOUT; o += NT) out[o] = __int_as_float(0x7fc00000);
       continue;
     }
+    // the next path's operand into the other buffer (its last readers, the
+    // previous path's steps, finished before the closing __syncthreads)
+    const int next = item + gridDim.x;
+    if (next < total) {
+      if (tid == 0) {
+        tc::fence_proxy_async();
+        tc::mbar_expect_tx(&full[b ^ 1], G::slot_bytes);
+        tc::bulk_g2s(smem + (size_t)(b ^ 1) * G::slot_bytes, L.opnd + (size_t)next * G::slot_bytes, G::slot_bytes,
+                     &full[b ^ 1]);
+      }
+      ++pending;
+    }
+    if (t.phi != cur_phi) {
+      // the group's low-pass factors (one filter per group in practice):
+      // T_r split into the step-3 B operand, T_c kept in fp32.  The previous
+      // step 3 has completed (its barrier wait precedes the last __syncthreads).
+      cur_phi = t.phi;
+      const float* trm = LP.r[t.phi];
+      for (int e = tid; e < N3 * (K3 / 8); e += NT) {
+        const int p = e % N3, c = e / N3;
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int kk = 8 * c + i;
+          v[i] = (p < NOUT && kk < M) ? __ldg(trm + p * M + kk) : 0.f;
+        }
+        dft::store_chunk(smem + G::off_b3h, smem + G::off_b3l, p, 8 * c, K3, v);
+      }
+      const float* tcm = LP.c[t.phi];
+      for (int e = tid; e < NOUT * M; e += NT) tcs[e / M * G::TCLD + e % M] = __ldg(tcm + e);
+      tc::fence_proxy_async();
+      __syncthreads();
+    }
+    alive = dft::cta_wait(&full[b], (uint32_t)(k >> 1) & 1u, status);
+    --pending;
+    if (!alive) {
+      for (int o = tid; o < NOUT * NOUT; o += NT) out[o] = __int_as_float(0x7fc00000);
+      continue;
+    }
     // ---- step 1: Z = A W ---------------------------------------------------------
-    dft::load_fold<M, KF, NT, MP>(ah, al, L, F, t, img);
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
     tc::fence_after_sync();
     if (tid == 0) {
       dft::split_gemm(taddr, s_ah, s_al, s_wh, s_wl, G::SBO, idesc1, KP / 16);
@@ -266,8 +435,8 @@ __global__ void __launch_bounds__(NT, 1)
       // K padding of the valid rows: k in [M, MP) and [MP + M, 2 MP)
       for (int e = tid; e < M * (MP - M) * 2; e += NT) {
         const int y = e / (2 * (MP - M)), r = e % (2 * (MP - M));
-        const int k = r < MP - M ? M + r : MP + M + (r - (MP - M));
-        dft::store_one(ah, al, y, k, KP, 0.f);
+        const int kk = r < MP - M ? M + r : MP + M + (r - (MP - M));
+        dft::store_one(ah, al, y, kk, KP, 0.f);
       }
     }
     tc::fence_proxy_async();
@@ -286,7 +455,7 @@ __global__ void __launch_bounds__(NT, 1)
       continue;
     }
     tc::fence_after_sync();
-    // ---- modulus -> step-3 operand (row y, K = x); T_r -> B operand ------------------
+    // ---- modulus -> step-3 operand (row y, K = x) -----------------------------------
     if (32 * quarter < M) {
       const int y = 32 * quarter + lane;
       const uint32_t lrow = taddr + ((uint32_t)(32 * quarter) << 16);
@@ -298,25 +467,12 @@ __global__ void __launch_bounds__(NT, 1)
           tc::tmem_ld8(lrow + (uint32_t)(MP + 8 * c), im);
           tc::tmem_wait_ld();
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = (8 * c + i < M) ? sqrtf(fmaf(re[i], re[i], im[i] * im[i])) : 0.f;
+          for (int i = 0; i < 8; ++i) v[i] = (8 * c + i < M) ? dft::sqrt_approx(fmaf(re[i], re[i], im[i] * im[i])) : 0.f;
         } else {
 #pragma unroll
           for (int i = 0; i < 8; ++i) v[i] = 0.f;
         }
-        if (y < M) dft::store_chunk(smem + G::off_a3h, smem + G::off_a3l, y, 8 * c, K3, v);
-      }
-    }
-    {
-      const float* trm = LP.r[t.phi];
-      for (int e = tid; e < N3 * (K3 / 8); e += NT) {
-        const int p = e % N3, c = e / N3;
-        float v[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int k = 8 * c + i;
-          v[i] = (p < NOUT && k < M) ? __ldg(trm + p * M + k) : 0.f;
-        }
-        dft::store_chunk(smem + G::off_b3h, smem + G::off_b3l, p, 8 * c, K3, v);
+        if (y < M) dft::store_chunk(buf, buf + G::off_a3l, y, 8 * c, K3, v);
       }
     }
     tc::fence_proxy_async();
@@ -352,35 +508,54 @@ __global__ void __launch_bounds__(NT, 1)
     tc::fence_before_sync();
     __syncthreads();
     // ---- S = T_c-contraction of T' on the FP32 pipe ------------------------------------
-    {
-      const float* tcm = LP.c[t.phi];
-      for (int o = tid; o < NOUT * NOUT; o += NT) {
-        const int p = o / NOUT, q = o % NOUT;
-        const float* tq = tcm + q * M;
-        float acc0 = 0.f, acc1 = 0.f;
+    // outputs o and o + NOUT^2 / 2 share q (and so their T_c row)
+    constexpr int HALF = NOUT * NOUT / 2;
+    static_assert((NOUT * NOUT) % 2 == 0 && HALF % NOUT == 0, "paired outputs share their column");
+    for (int o = tid; o < HALF; o += NT) {
+      const int p = o / NOUT, q = o % NOUT, p2 = p + HALF / NOUT;
+      const float* tq = tcs + q * G::TCLD;
+      float acc0 = 0.f, acc1 = 0.f;
 #pragma unroll 4
-        for (int y = 0; y < M; y += 2) {
-          acc0 = fmaf(__ldg(tq + y), Tp[y * TLD + p], acc0);
-          acc1 = fmaf(__ldg(tq + y + 1), Tp[(y + 1) * TLD + p], acc1);
-        }
-        out[o] = acc0 + acc1;
+      for (int y = 0; y < M; ++y) {
+        const float c = tq[y];
+        acc0 = fmaf(c, Tp[y * TLD + p], acc0);
+        acc1 = fmaf(c, Tp[y * TLD + p2], acc1);
       }
+      out[o] = acc0;
+      out[o + HALF] = acc1;
     }
-    __syncthreads();  // T' is overwritten by the next task's operands
+    __syncthreads();  // T' is overwritten by the path after next's operand copy
   }
+  // an operand copy still in flight (only after a time-out): wait for it (bounded)
+  if (pending > 0) tc::mbar_wait_bounded(&full[k & 1], (uint32_t)(k >> 1) & 1u, 1u << 22);
   tc::fence_before_sync();
   __syncthreads();
   if (tid < 32) tc::tmem_dealloc(taddr, G::TMEM_COLS);
 }
 
-// Launcher: the DFT operand image of size M for the current device
-// (built once), a persistent grid of one CTA per SM.
+// Launcher: the fold pass into the operand slots (L.opnd), then the GEMM
+// kernel on a persistent grid of one CTA per SM with the DFT operand image
+// of size M for the current device (built once).
 const unsigned char* dft_operand_image(int m, size_t bytes);
+
+template <int M, int KF, int P, int Q>
+cudaError_t launch_fold(const CascadeLaunch& L, const FilterTable& F, unsigned* status, int nimg,
+                        cudaStream_t stream) {
+  using S = StripGeom<M, KF, P, Q>;
+  auto kern = tcdft_fold_kernel<M, KF, P, Q>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem);
+  if (e != cudaSuccess) return e;
+  kern<<<dim3(M, nimg, 1), S::NT, S::smem, stream>>>(L, F, status);
+  return cudaGetLastError();
+}
 
 template <int M, int NOUT, int KF, int NT>
 cudaError_t tcdft_launch(const CascadeLaunch& L, const FilterTable& F, const LowpassTable& LP, unsigned* status,
                          int nimg, cudaStream_t stream) {
   using G = DftGeom<M, NOUT>;
+  if (!L.opnd) return cudaErrorInvalidValue;
+  const int total = L.ntasks * nimg;
+  if (total <= 0) return cudaSuccess;
   auto kern = tcdft_cascade_kernel<M, NOUT, KF, NT>;
   const unsigned char* w = dft_operand_image(M, G::w_bytes);
   if (!w) return cudaErrorMemoryAllocation;
@@ -391,10 +566,13 @@ cudaError_t tcdft_launch(const CascadeLaunch& L, const FilterTable& F, const Low
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
   if (e != cudaSuccess) return e;
-  const int total = L.ntasks * nimg;
-  if (total <= 0) return cudaSuccess;
+  // the fold pass over the P x Q grid of paths (Q = 8 wavelets; P = 1 or 8 sources)
+  if (L.ntasks == 8) e = launch_fold<M, KF, 1, 8>(L, F, status, nimg, stream);
+  else if (L.ntasks == 64) e = launch_fold<M, KF, 8, 8>(L, F, status, nimg, stream);
+  else e = cudaErrorInvalidValue;
+  if (e != cudaSuccess) return e;
   const int grid = total < sms ? total : sms;
-  kern<<<grid, NT, G::smem, stream>>>(L, F, LP, w, nimg, status);
+  kern<<<grid, NT, G::smem, stream>>>(L, LP, w, nimg, status);
   return cudaGetLastError();
 }
 

@@ -236,13 +236,12 @@ class Scattering1D(nn.Module):
             raise ValueError("Cannot convert to out_type='array' with T=0. Please set out_type to 'dict' or 'list'.")
         if len(x.shape) < 1:
             raise ValueError('Input tensor x should have at least one axis, got {}'.format(len(x.shape)))
-        if self.average != 'local':
-            raise NotImplementedError('the GB300 engine runs the locally averaged transform (T a number or '
-                                      'None); T=0 and T="global" are not available in this build')
         if not x.is_cuda:
             raise TypeError('The input must be a CUDA tensor: the GB300 scattering engine runs on CUDA only.')
         if x.dtype != torch.float32:
             raise TypeError('The input must be float32 (got %s).' % x.dtype)
+        if self.average != 'local':
+            return self._scattering_unaveraged(x)
         batch_shape = x.shape[:-1]
         xb = x.reshape((-1, x.shape[-1]))
         S = _autograd.CascadeFn.apply(xb, self)
@@ -257,6 +256,56 @@ class Scattering1D(nn.Module):
             j = tuple(self.psi1_f[k[0]]['j'] if i == 0 else self.psi2_f[k[1]]['j'] for i in range(len(k)))
             out.append({'coef': S[..., c, :], 'j': j, 'n': k, 'order': len(k)})
         return out
+
+    def _op_filters(self):
+        """The registered buffers as the filter dicts of the op-level cascade:
+        [phi, psi1 bank, psi2 bank] with 'levels' the device tensors."""
+        n = 0
+        phi = dict(self.phi_f)
+        phi['levels'] = [getattr(self, 'tensor%d' % (n + i)) for i in range(self._nlev['phi'])]
+        n += self._nlev['phi']
+        banks = []
+        for key, meta in (('psi1', self.psi1_f), ('psi2', self.psi2_f)):
+            bank = []
+            for p, nl in zip(meta, self._nlev[key]):
+                d = dict(p)
+                d['levels'] = [getattr(self, 'tensor%d' % (n + i)) for i in range(nl)]
+                n += nl
+                bank.append(d)
+            banks.append(bank)
+        return [phi] + banks
+
+    def _scattering_unaveraged(self, x):
+        """T=0 (no averaging) and T='global' (sum over time), run op by op on
+        this package's CUDA op surface (``backend1d``): the reference frontend
+        kymatio/scattering1d/frontend/base_frontend.py:108-155 over the core
+        kymatio/scattering1d/core/scattering1d.py:2-107 with average_local
+        False.  Gradients flow through the ops' autograd rules."""
+        from . import core
+        from .backend import backend1d as B
+        batch_shape = tuple(x.shape[:-1])
+        signal_shape = tuple(x.shape[-1:])
+        U_0 = B.pad(B.reshape_input(x.contiguous(), signal_shape), pad_left=self.pad_left, pad_right=self.pad_right)
+        filters = self._op_filters()[:1 + self.max_order]
+        S = {} if self.out_type == 'dict' else []
+        for path in core.scattering1d(U_0, B, filters, self.J, False):
+            path['order'] = len(path['n'])
+            res = max(path['j'][-1] - self._oversampling, 0) if path['order'] > 0 else 0
+            if self.average == 'global':
+                coef = B.average_global(path['coef'])
+            else:
+                coef = B.unpad(path['coef'], self.ind_start[res], self.ind_end[res])
+            path['coef'] = B.reshape_output(coef, batch_shape, n_kept_dims=1)
+            if self.out_type == 'dict':
+                S[path['n']] = path['coef']
+            else:
+                S.append(path)
+        if self.out_type == 'dict':
+            return S
+        S.sort(key=lambda p: (p['order'], p['n']))
+        if self.out_type == 'array':
+            return B.stack([p['coef'] for p in S], dim=-2)
+        return S
 
     def _forward_raw(self, x):
         plan = self._get_plan()

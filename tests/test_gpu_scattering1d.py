@@ -53,9 +53,15 @@ def test_reference_cases(case):
         kw['Q'] = tuple(kw['Q'])
     S = Scattering1D(**kw).to(dev)
     x = torch.from_numpy(d[case['name'] + '/x']).to(dev)
-    if S.average != 'local':
-        with pytest.raises(NotImplementedError):
-            S(x)
+    if S.average is False:
+        # T=0: un-averaged paths U at their own resolutions, keyed by n
+        out = S(x)
+        assert isinstance(out, list) and len(out) == S.output_size()
+        for p in out:
+            ref = d[case['name'] + '/S/' + ','.join(str(n) for n in p['n'])]
+            got = p['coef'].cpu().numpy()
+            assert got.shape == ref.shape, (p['n'], got.shape, ref.shape)
+            assert rel_l2(got, ref) <= 1e-5, (p['n'], rel_l2(got, ref))
         return
     out = S(x).cpu().numpy()
     ref = d[case['name'] + '/S']
