@@ -377,14 +377,20 @@ def run_ours(args, world, rank, local):
     if rank == 0 and not args.no_cpu:
         from oracle.scattering2d import Scattering2D as Oracle
         ref = Oracle(J, (SIDE, SIDE), L=L)(x_np[:2].astype(np.float64))
-        for form in ('plain', 'tc'):
-            step(form, False)
+        for form in ('plain', 'tc', 'tc_dft'):
+            prev = lib.kym_set_tc_dft(1 if form == 'tc_dft' else 0)
+            step('plain' if form == 'plain' else 'tc', False)
             torch.cuda.synchronize()
+            lib.kym_set_tc_dft(prev)
             prec[form] = order_rel_l2(out[:2].cpu().numpy(), ref)
     sampler = ClockSampler(local)
     sampler.start()
     t_plain, g_plain = measure('plain')
     t_tc, g_tc = measure('tc')
+    # the DFT-GEMM form of the 68x68 groups (opt-in), measured beside the default form
+    prev_dft = lib.kym_set_tc_dft(1)
+    t_dft, g_dft = measure('tc')
+    lib.kym_set_tc_dft(prev_dft)
     clocks = sampler.stop()
     tc_status = S.tensor_core_status()
     value = BATCH * world / (t_tc / 1e3)
@@ -475,6 +481,12 @@ def run_ours(args, world, rank, local):
                            'rel_l2_vs_fp64': prec.get('plain'),
                            'group_ms_per_step': [round(v, 4) for v in g_plain]},
             'tc_vs_plain': value / value_plain,
+            'tc_dft_gemm': {'value': BATCH * world / (t_dft / 1e3), 'unit': 'img/s', 'ms_per_step': t_dft,
+                            'rel_l2_vs_fp64': prec.get('tc_dft'),
+                            'group_ms_per_step': [round(v, 4) for v in g_dft],
+                            'groups': 'the 68x68 groups (order 1 j1=2, order 2 (0,2) and (1,2)) as DFT-GEMMs '
+                                      'on tcgen05 after a shared-source fold pass; other groups as in the '
+                                      'tensor-core form'},
             'rel_l2_vs_fp64': prec.get('tc'), 'rel_l2_orders': ['S0', 'S1', 'S2'],
             'tc_status': tc_status,
             'e2e': {'value': e2e, 'unit': 'img/s', 'h2d_bytes_per_step': int(x_host.numel() * 4),
