@@ -65,12 +65,12 @@ struct DftGeom {
   static constexpr int MAX_TASKS = 64;
   static constexpr size_t off_tasks = (off_tc + (size_t)NOUT * TCLD * 4 + 15) / 16 * 16;
   static constexpr size_t bar_off = off_tasks + (size_t)MAX_TASKS * sizeof(Task);
-  static constexpr size_t smem = bar_off + 48;  // wbar, mbar, full[2], TMEM base
+  static constexpr size_t smem = bar_off + 48;  // wbar, mbar[2], full[2], TMEM base
   static constexpr int C3 = (NP + 31) / 32 * 32;  // TMEM column of D3
-  static constexpr int TMEM_COLS = 256;
+  static constexpr int TMEM_COLS = 512;  // two groups, 256 columns each
   static constexpr uint32_t w_bytes = (uint32_t)(2 * w_half);
   static_assert(M % 4 == 0 && M <= 120, "work size");
-  static_assert(NP <= 256 && C3 + N3 <= TMEM_COLS, "accumulator tile too wide");
+  static_assert(NP <= 256 && C3 + N3 <= TMEM_COLS / 2, "accumulator tile too wide");
   static_assert(2 * half_a3 <= slot_bytes && (size_t)M * TLD * 4 <= slot_bytes,
                 "step-3 operand and T' fit the path's buffer");
   static_assert(slot_bytes % 16 == 0, "TMA bulk copies move multiples of 16 bytes");
@@ -284,23 +284,57 @@ __global__ void __launch_bounds__(StripGeom<M, KF, P, Q>::NT)
   }
 }
 
-// The GEMM kernel: persistent, one CTA per SM.  Path k of the CTA arrives in
-// buffer k & 1 by TMA bulk copy, issued while path k - 1 is computed.
+// The GEMM kernel: persistent, one CTA per SM, split into two independent
+// groups of 8 warps.  Group g computes paths blockIdx.x + (2k + g) gridDim.x
+// in its own operand buffer and its own half of tensor memory, with its own
+// barriers, so one group's GEMMs run while the other reads back, and each
+// group's next operand copy (TMA bulk copy) lands while the other computes.
+namespace dft {
+// named barrier of one group (ids 1 and 2; 0 is __syncthreads)
+__device__ __forceinline__ void grp_sync(int g) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(256) : "memory");
+}
+__device__ __forceinline__ bool grp_any(int g, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(1 + g), "r"(256)
+      : "memory");
+  return r != 0;
+}
+// group-wide bounded wait; on a time-out the status word is flagged and the
+// group waits once more (bounded) for the operations it issued
+__device__ __forceinline__ bool grp_wait(int g, uint64_t* bar, uint32_t parity, unsigned* status) {
+  const bool ok = tc::mbar_wait_bounded(bar, parity, 1u << 22);
+  if (grp_any(g, !ok)) {
+    if ((threadIdx.x & 255) == 0) atomicOr(status, tc::kErrMmaTimeout);
+    tc::mbar_wait_bounded(bar, parity, 1u << 22);
+    grp_sync(g);
+    return false;
+  }
+  return true;
+}
+}  // namespace dft
+
 template <int M, int NOUT, int KF, int NT>
 __global__ void __launch_bounds__(NT, 1)
     tcdft_cascade_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ LowpassTable LP,
                          const unsigned char* __restrict__ wimg, int nimg, unsigned* status) {
   using G = DftGeom<M, NOUT>;
   constexpr int MP = G::MP, KP = G::KP, NP = G::NP, K3 = G::K3, N3 = G::N3, TLD = G::TLD;
-  constexpr int NCH = MP / 8;        // 8-column chunks of one [Re | Im] half
-  constexpr int WPQ = NT / 128;      // warps per TMEM lane quarter
-  static_assert(NT % 128 == 0, "whole lane quarters");
+  constexpr int NCH = MP / 8;  // 8-column chunks of one [Re | Im] half
+  constexpr int GT = 256;      // threads per group
+  constexpr int WPQ = 2;       // warps per TMEM lane quarter within a group
+  static_assert(NT == 2 * GT, "two groups of 8 warps");
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* wbar = reinterpret_cast<uint64_t*>(smem + G::bar_off);
-  uint64_t* mbar = wbar + 1;
-  uint64_t* full = wbar + 2;  // full[0], full[1]
-  uint32_t* slot = reinterpret_cast<uint32_t*>(smem + G::bar_off + 32);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint64_t* mbar = wbar + 1;  // mbar[0], mbar[1]: GEMM completion per group
+  uint64_t* full = wbar + 3;  // full[0], full[1]: operand arrival per group
+  uint32_t* slot = reinterpret_cast<uint32_t*>(smem + G::bar_off + 40);
+  const int tid = threadIdx.x;
+  const int g = tid / GT, gtid = tid % GT;
+  const int warp = gtid >> 5, lane = tid & 31;
   const int quarter = warp & 3, cgroup = warp >> 2;
   const int total = L.ntasks * nimg;
 
@@ -310,103 +344,89 @@ __global__ void __launch_bounds__(NT, 1)
   }
   if (tid == 0) {
     tc::mbar_init(wbar, 1);
-    tc::mbar_init(mbar, 1);
-    tc::mbar_init(&full[0], 1);
-    tc::mbar_init(&full[1], 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&mbar[i], 1);
+      tc::mbar_init(&full[i], 1);
+    }
     tc::mbar_fence_init();
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t taddr = *slot;
+  const uint32_t taddr = *slot + (uint32_t)(g * (G::TMEM_COLS / 2));  // this group's half
   if (tid == 0) {
-    // the resident DFT matrix, then the first path's operand
+    // the resident DFT matrix, then each group's first operand
     tc::mbar_expect_tx(wbar, G::w_bytes);
     for (uint32_t o = 0; o < G::w_bytes; o += 16384u)
       tc::bulk_g2s(smem + G::off_wh + o, wimg + o, (G::w_bytes - o) < 16384u ? (G::w_bytes - o) : 16384u, wbar);
-    if ((int)blockIdx.x < total) {
-      tc::mbar_expect_tx(&full[0], G::slot_bytes);
-      tc::bulk_g2s(smem, L.opnd + (size_t)blockIdx.x * G::slot_bytes, G::slot_bytes, &full[0]);
+    for (int i = 0; i < 2; ++i) {
+      const int first = (int)blockIdx.x + i * (int)gridDim.x;
+      if (first < total) {
+        tc::mbar_expect_tx(&full[i], G::slot_bytes);
+        tc::bulk_g2s(smem + (size_t)i * G::slot_bytes, L.opnd + (size_t)first * G::slot_bytes, G::slot_bytes,
+                     &full[i]);
+      }
     }
   }
+  // the group's low-pass factors (one filter per group, checked when the plan
+  // was made): T_r split into the step-3 B operand, T_c kept in fp32; the task table
+  float* tcs = reinterpret_cast<float*>(smem + G::off_tc);
+  Task* tasks = reinterpret_cast<Task*>(smem + G::off_tasks);
+  for (int i = tid; i < L.ntasks; i += NT) tasks[i] = L.tasks[i];
+  {
+    const int phi = L.tasks[0].phi;
+    const float* trm = LP.r[phi];
+    for (int e = tid; e < N3 * (K3 / 8); e += NT) {
+      const int p = e % N3, c = e / N3;
+      float v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int kk = 8 * c + i;
+        v[i] = (p < NOUT && kk < M) ? __ldg(trm + p * M + kk) : 0.f;
+      }
+      dft::store_chunk(smem + G::off_b3h, smem + G::off_b3l, p, 8 * c, K3, v);
+    }
+    const float* tcm = LP.c[phi];
+    for (int e = tid; e < NOUT * M; e += NT) tcs[e / M * G::TCLD + e % M] = __ldg(tcm + e);
+  }
+  tc::fence_proxy_async();
+  bool alive = dft::cta_wait(wbar, 0, status);  // CTA-wide: includes the barrier for the tables above
+
   const uint32_t s_wh = tc::smem_addr(smem + G::off_wh), s_wl = tc::smem_addr(smem + G::off_wl);
   const uint32_t s_b3h = tc::smem_addr(smem + G::off_b3h), s_b3l = tc::smem_addr(smem + G::off_b3l);
   constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, NP);
   constexpr uint32_t idesc3 = tc::idesc_bf16_f32(128, N3);
-  float* tcs = reinterpret_cast<float*>(smem + G::off_tc);
-  Task* tasks = reinterpret_cast<Task*>(smem + G::off_tasks);
-  for (int i = tid; i < L.ntasks; i += NT) tasks[i] = L.tasks[i];
-  __syncthreads();
-
-  uint32_t ph = 0;
-  int cur_phi = -1;
-  int pending = (int)blockIdx.x < total ? 1 : 0;  // operand copies issued and not yet waited for
-  bool alive = dft::cta_wait(wbar, 0, status);
-  int k = 0;
-  for (int item = blockIdx.x; item < total; item += gridDim.x, ++k) {
-    const int b = k & 1;
-    unsigned char* buf = smem + (size_t)b * G::slot_bytes;
-    unsigned char* ah = buf;
-    unsigned char* al = buf + G::half_a;
-    const uint32_t s_ah = tc::smem_addr(ah), s_al = tc::smem_addr(al);
-    const uint32_t s_a3h = s_ah, s_a3l = s_ah + (uint32_t)G::off_a3l;
-    float* Tp = reinterpret_cast<float*>(buf);
+  unsigned char* buf = smem + (size_t)g * G::slot_bytes;
+  unsigned char* ah = buf;
+  unsigned char* al = buf + G::half_a;
+  const uint32_t s_ah = tc::smem_addr(ah), s_al = tc::smem_addr(al);
+  const uint32_t s_a3h = s_ah, s_a3l = s_ah + (uint32_t)G::off_a3l;
+  float* Tp = reinterpret_cast<float*>(buf);
+  uint32_t ph = 0, fph = 0;
+  bool pending = (int)blockIdx.x + g * (int)gridDim.x < total;  // an operand copy is in flight
+  for (int item = blockIdx.x + g * gridDim.x; item < total; item += 2 * gridDim.x) {
     const int img = item / L.ntasks;
     const Task t = tasks[item - img * L.ntasks];
     float* out = L.out + (size_t)(L.img0 + img) * L.out_stride + (size_t)t.out_ch * NOUT * NOUT;
+    if (alive) {
+      alive = dft::grp_wait(g, &full[g], fph, status);
+      fph ^= 1u;
+      pending = false;
+    }
     if (!alive) {
-      for (int o = tid; o < NOUT * NOUT; o += NT) out[o] = __int_as_float(0x7fc00000);
-      continue;
-    }
-    // the next path's operand into the other buffer (its last readers, the
-    // previous path's steps, finished before the closing __syncthreads)
-    const int next = item + gridDim.x;
-    if (next < total) {
-      if (tid == 0) {
-        tc::fence_proxy_async();
-        tc::mbar_expect_tx(&full[b ^ 1], G::slot_bytes);
-        tc::bulk_g2s(smem + (size_t)(b ^ 1) * G::slot_bytes, L.opnd + (size_t)next * G::slot_bytes, G::slot_bytes,
-                     &full[b ^ 1]);
-      }
-      ++pending;
-    }
-    if (t.phi != cur_phi) {
-      // the group's low-pass factors (one filter per group in practice):
-      // T_r split into the step-3 B operand, T_c kept in fp32.  The previous
-      // step 3 has completed (its barrier wait precedes the last __syncthreads).
-      cur_phi = t.phi;
-      const float* trm = LP.r[t.phi];
-      for (int e = tid; e < N3 * (K3 / 8); e += NT) {
-        const int p = e % N3, c = e / N3;
-        float v[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int kk = 8 * c + i;
-          v[i] = (p < NOUT && kk < M) ? __ldg(trm + p * M + kk) : 0.f;
-        }
-        dft::store_chunk(smem + G::off_b3h, smem + G::off_b3l, p, 8 * c, K3, v);
-      }
-      const float* tcm = LP.c[t.phi];
-      for (int e = tid; e < NOUT * M; e += NT) tcs[e / M * G::TCLD + e % M] = __ldg(tcm + e);
-      tc::fence_proxy_async();
-      __syncthreads();
-    }
-    alive = dft::cta_wait(&full[b], (uint32_t)(k >> 1) & 1u, status);
-    --pending;
-    if (!alive) {
-      for (int o = tid; o < NOUT * NOUT; o += NT) out[o] = __int_as_float(0x7fc00000);
+      for (int o = gtid; o < NOUT * NOUT; o += GT) out[o] = __int_as_float(0x7fc00000);
       continue;
     }
     // ---- step 1: Z = A W ---------------------------------------------------------
     tc::fence_after_sync();
-    if (tid == 0) {
+    if (gtid == 0) {
       dft::split_gemm(taddr, s_ah, s_al, s_wh, s_wl, G::SBO, idesc1, KP / 16);
-      tc::mma_commit(mbar);
+      tc::mma_commit(&mbar[g]);
     }
-    alive = dft::cta_wait(mbar, ph, status);
+    alive = dft::grp_wait(g, &mbar[g], ph, status);
     ph ^= 1u;
     if (!alive) {
-      for (int o = tid; o < NOUT * NOUT; o += NT) out[o] = __int_as_float(0x7fc00000);
+      for (int o = gtid; o < NOUT * NOUT; o += GT) out[o] = __int_as_float(0x7fc00000);
       continue;
     }
     tc::fence_after_sync();
@@ -433,7 +453,7 @@ __global__ void __launch_bounds__(NT, 1)
     }
     if constexpr (MP > M) {
       // K padding of the valid rows: k in [M, MP) and [MP + M, 2 MP)
-      for (int e = tid; e < M * (MP - M) * 2; e += NT) {
+      for (int e = gtid; e < M * (MP - M) * 2; e += GT) {
         const int y = e / (2 * (MP - M)), r = e % (2 * (MP - M));
         const int kk = r < MP - M ? M + r : MP + M + (r - (MP - M));
         dft::store_one(ah, al, y, kk, KP, 0.f);
@@ -441,17 +461,17 @@ __global__ void __launch_bounds__(NT, 1)
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
-    __syncthreads();
+    dft::grp_sync(g);
     tc::fence_after_sync();
     // ---- step 2: U^T = Z^T W ------------------------------------------------------
-    if (tid == 0) {
+    if (gtid == 0) {
       dft::split_gemm(taddr, s_ah, s_al, s_wh, s_wl, G::SBO, idesc1, KP / 16);
-      tc::mma_commit(mbar);
+      tc::mma_commit(&mbar[g]);
     }
-    alive = dft::cta_wait(mbar, ph, status);
+    alive = dft::grp_wait(g, &mbar[g], ph, status);
     ph ^= 1u;
     if (!alive) {
-      for (int o = tid; o < NOUT * NOUT; o += NT) out[o] = __int_as_float(0x7fc00000);
+      for (int o = gtid; o < NOUT * NOUT; o += GT) out[o] = __int_as_float(0x7fc00000);
       continue;
     }
     tc::fence_after_sync();
@@ -477,17 +497,17 @@ __global__ void __launch_bounds__(NT, 1)
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
-    __syncthreads();
+    dft::grp_sync(g);
     tc::fence_after_sync();
     // ---- step 3: T' = U^T T_r^T ------------------------------------------------------
-    if (tid == 0) {
+    if (gtid == 0) {
       dft::split_gemm(taddr + (uint32_t)G::C3, s_a3h, s_a3l, s_b3h, s_b3l, G::SBO3, idesc3, K3 / 16);
-      tc::mma_commit(mbar);
+      tc::mma_commit(&mbar[g]);
     }
-    alive = dft::cta_wait(mbar, ph, status);
+    alive = dft::grp_wait(g, &mbar[g], ph, status);
     ph ^= 1u;
     if (!alive) {
-      for (int o = tid; o < NOUT * NOUT; o += NT) out[o] = __int_as_float(0x7fc00000);
+      for (int o = gtid; o < NOUT * NOUT; o += GT) out[o] = __int_as_float(0x7fc00000);
       continue;
     }
     tc::fence_after_sync();
@@ -506,12 +526,12 @@ __global__ void __launch_bounds__(NT, 1)
       }
     }
     tc::fence_before_sync();
-    __syncthreads();
+    dft::grp_sync(g);
     // ---- S = T_c-contraction of T' on the FP32 pipe ------------------------------------
     // outputs o and o + NOUT^2 / 2 share q (and so their T_c row)
     constexpr int HALF = NOUT * NOUT / 2;
     static_assert((NOUT * NOUT) % 2 == 0 && HALF % NOUT == 0, "paired outputs share their column");
-    for (int o = tid; o < HALF; o += NT) {
+    for (int o = gtid; o < HALF; o += GT) {
       const int p = o / NOUT, q = o % NOUT, p2 = p + HALF / NOUT;
       const float* tq = tcs + q * G::TCLD;
       float acc0 = 0.f, acc1 = 0.f;
@@ -524,13 +544,22 @@ __global__ void __launch_bounds__(NT, 1)
       out[o] = acc0;
       out[o + HALF] = acc1;
     }
-    __syncthreads();  // T' is overwritten by the path after next's operand copy
+    dft::grp_sync(g);  // T' is dead: the buffer takes the group's next operand
+    const int next = item + 2 * gridDim.x;
+    if (next < total) {
+      if (gtid == 0) {
+        tc::fence_proxy_async();
+        tc::mbar_expect_tx(&full[g], G::slot_bytes);
+        tc::bulk_g2s(buf, L.opnd + (size_t)next * G::slot_bytes, G::slot_bytes, &full[g]);
+      }
+      pending = true;
+    }
   }
   // an operand copy still in flight (only after a time-out): wait for it (bounded)
-  if (pending > 0) tc::mbar_wait_bounded(&full[k & 1], (uint32_t)(k >> 1) & 1u, 1u << 22);
+  if (pending) tc::mbar_wait_bounded(&full[g], fph, 1u << 22);
   tc::fence_before_sync();
   __syncthreads();
-  if (tid < 32) tc::tmem_dealloc(taddr, G::TMEM_COLS);
+  if (tid < 32) tc::tmem_dealloc(*slot, G::TMEM_COLS);
 }
 
 // Launcher: the fold pass into the operand slots (L.opnd), then the GEMM
