@@ -2,7 +2,7 @@
 // (work 136/68, output 32x32), 32/64/128 inputs with a 10x10 low-pass
 // (work 80/40/20, output 8x8) and 256x256 at J=4 (work 144/72/36, output 16x16).
 #include "tc_cascade.cuh"
-KYM_TC_VARIANT(136, 136, 32, 32, 2, 512)
+KYM_TC_VARIANT(136, 136, 32, 32, 2, 640)
 KYM_TC_VARIANT(68, 68, 32, 32, 4, 512)
 KYM_TC_VARIANT(68, 68, 32, 32, 2, 512)
 KYM_TC_VARIANT(80, 80, 8, 8, 2, 512)
