@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
           float uv = 0.f;
           if (k < MC) {
             const float2 z = A[r * LD + k];
-            uv = sqrtf(fmaf(z.x, z.x, z.y * z.y));
+            uv = tc::sqrt_approx(fmaf(z.x, z.x, z.y * z.y));
           }
           __nv_bfloat16 bh, bl;
           tc::split_bf16(uv, bh, bl);
@@ -225,16 +225,30 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
 
   // ---- S = T_r * T on the FP32 pipe, written to the output channel -----------------
   float* out = L.out + (size_t)(L.img0 + img) * L.out_stride + (size_t)t.out_ch * NOUTR * NOUTC;
-  for (int o = tid; o < NOUTR * NOUTC; o += NT) {
+  // rows p and p + NOUTR / 2 share their T loads; four independent chains
+  constexpr int HR = NOUTR / 2;
+  static_assert(NOUTR % 2 == 0 && MR % 4 == 0, "paired rows and 16-byte T_r loads");
+  for (int o = tid; o < HR * NOUTC; o += NT) {
     const int p = o / NOUTC, q = o % NOUTC;
-    const float* tr = trs + p * MR;
-    float acc0 = 0.f, acc1 = 0.f;
-#pragma unroll 4
-    for (int x = 0; x < MR; x += 2) {
-      acc0 = fmaf(tr[x], T[x * TLD + q], acc0);
-      if (x + 1 < MR) acc1 = fmaf(tr[x + 1], T[(x + 1) * TLD + q], acc1);
+    const float4* r0 = reinterpret_cast<const float4*>(trs + p * MR);
+    const float4* r1 = reinterpret_cast<const float4*>(trs + (p + HR) * MR);
+    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+#pragma unroll 2
+    for (int x4 = 0; x4 < MR / 4; ++x4) {
+      const float4 u = r0[x4], w = r1[x4];
+      const float* tq = T + 4 * x4 * TLD + q;
+      const float t0 = tq[0], t1 = tq[TLD], t2 = tq[2 * TLD], t3 = tq[3 * TLD];
+      a0 = fmaf(u.x, t0, a0);
+      a1 = fmaf(u.y, t1, a1);
+      b0 = fmaf(w.x, t0, b0);
+      b1 = fmaf(w.y, t1, b1);
+      a0 = fmaf(u.z, t2, a0);
+      a1 = fmaf(u.w, t3, a1);
+      b0 = fmaf(w.z, t2, b0);
+      b1 = fmaf(w.w, t3, b1);
     }
-    out[o] = ok ? acc0 + acc1 : __int_as_float(0x7fc00000);
+    out[p * NOUTC + q] = ok ? a0 + a1 : __int_as_float(0x7fc00000);
+    out[(p + HR) * NOUTC + q] = ok ? b0 + b1 : __int_as_float(0x7fc00000);
   }
 }
 

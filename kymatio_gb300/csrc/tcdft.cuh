@@ -105,14 +105,6 @@ __device__ __forceinline__ void store_one(unsigned char* hi, unsigned char* lo, 
   *reinterpret_cast<__nv_bfloat16*>(lo + off) = l;
 }
 
-// Hardware square root (sqrt.approx.f32, relative error about 2^-23): the
-// modulus feeds a BF16 hi/lo split, far coarser than its rounding.
-__device__ __forceinline__ float sqrt_approx(float x) {
-  float r;
-  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-
 // D (+)= A B^T over ksteps K-steps of 16, three split products per step.
 __device__ __forceinline__ void split_gemm(uint32_t d, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl,
                                            uint32_t sbo, uint32_t idesc, int ksteps) {
@@ -487,7 +479,7 @@ __global__ void __launch_bounds__(NT, 1)
           tc::tmem_ld8(lrow + (uint32_t)(MP + 8 * c), im);
           tc::tmem_wait_ld();
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = (8 * c + i < M) ? dft::sqrt_approx(fmaf(re[i], re[i], im[i] * im[i])) : 0.f;
+          for (int i = 0; i < 8; ++i) v[i] = (8 * c + i < M) ? tc::sqrt_approx(fmaf(re[i], re[i], im[i] * im[i])) : 0.f;
         } else {
 #pragma unroll
           for (int i = 0; i < 8; ++i) v[i] = 0.f;
