@@ -368,6 +368,28 @@ class TorchGB300Backend1D(TorchGB300Backend):
         cls.real_check(x)
         return torch.sum(x, axis=-2, keepdims=True)
 
+    # -- frequency-axis moves of time-frequency scattering
+    #    (kymatio/scattering1d/backend/torch_backend.py:150-223): views and copies
+    @classmethod
+    def pad_frequency(cls, x, padding):
+        """One-sided zero padding of the frequency axis (dim -2) to lower frequencies."""
+        return torch.nn.functional.pad(x, (0, 0, 0, padding), mode='constant', value=0)
+
+    @classmethod
+    def swap_time_frequency(cls, x):
+        """(..., frequency, time, 1|2) <-> (..., time, frequency, 1|2), contiguous."""
+        return torch.transpose(x, dim0=-2, dim1=-3).contiguous()
+
+    @staticmethod
+    def unpad_frequency(x, n1_max, n1_stride):
+        """Keep the 1 + n1_max // n1_stride first frequency bins (dim 2)."""
+        return x[:, :, :1 + (n1_max // n1_stride), :]
+
+    @staticmethod
+    def split_frequency_axis(x):
+        """One tensor per frequency bin (dim -3), each of size 1 there."""
+        return torch.split(x, 1, dim=-3)
+
 
 backend2d = TorchGB300Backend2D
 backend1d = TorchGB300Backend1D

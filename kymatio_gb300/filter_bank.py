@@ -190,6 +190,32 @@ def filter_bank_1d(N_padded, J, Q, T):
     return (phi,) + tuple(banks)
 
 
+@functools.lru_cache(maxsize=16)
+def filter_bank_fr(N_fr, J_fr, Q_fr, F):
+    """Frequency-axis filters of joint time-frequency scattering
+    (kymatio/scattering1d/frontend/base_frontend.py:570-579): returns
+    (phi_F, psis) where phi_F averages over F first-order channels and psis
+    is [phi_{2^J_fr}] followed by the Anden wavelets of (J_fr, Q_fr) with
+    positive center frequency, then the same wavelets mirrored to negative
+    frequency (the "spin" down; kymatio/scattering1d/filter_bank.py:314-319).
+    Levels are alias sums, as for the time filters."""
+    def lowpass(T, n_levels):
+        sigma = SIGMA0 / T
+        p0 = morlet_1d(N_fr, None, sigma)
+        levels = [p0] + [p0.reshape(2 ** l, -1).sum(axis=0) for l in range(1, n_levels)]
+        return {'levels': tuple(levels), 'xi': 0, 'sigma': sigma, 'j': int(math.floor(math.log2(T))), 'N': N_fr}
+
+    phi_F = lowpass(F, max(0, 1 + int(math.floor(math.log2(F)))))
+    pairs = anden_pairs(J_fr, Q_fr)
+    psis, max_j = [], 0
+    for xi, sigma in pairs + [(-xi, sigma) for xi, sigma in pairs]:
+        j = _max_subsampling(xi, sigma)
+        psis.append({'levels': (morlet_1d(N_fr, xi, sigma),), 'xi': xi, 'sigma': sigma, 'j': j})
+        max_j = max(max_j, j)
+    phi_J = lowpass(2 ** J_fr, max(max_j, 1 + J_fr))
+    return phi_F, (phi_J,) + tuple(psis)
+
+
 def geometry_1d(J, N_input, T):
     """Padding of ScatteringBase1D.build: (N_padded, pad_left, pad_right)."""
     phi_f = morlet_1d(N_input, None, SIGMA0 / T)

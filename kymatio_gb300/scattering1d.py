@@ -23,19 +23,21 @@ from .filter_bank import border_indices, filter_bank_1d, geometry_1d
 from .scattering2d import _Plan
 
 
-def _parse_T(T, J, N_input):
-    """kymatio/scattering1d/utils.py:75-107."""
+def _parse_T(T, J, N_input, T_alias='T'):
+    """kymatio/scattering1d/utils.py:71-108 (T_alias 'F' for the frequential
+    low-pass of time-frequency scattering)."""
     if T is None:
         return 2 ** J, 'local'
     if T == 'global':
         return 2 ** J, 'global'
     if T > N_input:
         raise ValueError("The support {} of the low-pass filter cannot exceed input length (got {} > {}). "
-                         "For large averaging size, consider passing T='global'.".format(T, T, N_input))
+                         "For large averaging size, consider passing {}='global'.".format(T_alias, T, N_input,
+                                                                                         T_alias))
     if T == 0:
         return 2 ** J, False
     if T < 1:
-        raise ValueError('T must be ==0 or >=1 (got {})'.format(T))
+        raise ValueError('{} must be ==0 or >=1 (got {})'.format(T_alias, T))
     return T, 'local'
 
 

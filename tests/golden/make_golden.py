@@ -20,7 +20,11 @@ on current scipy) and writes:
   checksums of the 272x272 J=3 bank;
 * ``ref_grads.npz`` -- input gradients from the reference torch frontend's
   autograd in float64 (x, upstream gradient g, d<g, S(x)>/dx) for 2-D and 1-D
-  configurations.
+  configurations;
+* ``ref_jtfs.npz`` -- seeded inputs and reference numpy FP64 outputs of joint
+  time-frequency scattering (formats 'time' and 'joint', out_type array, list
+  and dict, F local / zero / global, T global), with each configuration's
+  ``meta()`` (keys, order, n_fr, spin, frequential xi / sigma / j).
 
 Nothing at test time reads the reference; the tests read these files.
 """
@@ -162,7 +166,49 @@ def grads(ref_root):
     np.savez_compressed(os.path.join(HERE, 'ref_grads.npz'), **out)
 
 
+CASES_JTFS = [
+    # name, kwargs, batch
+    ('time_j6_jfr2_q82', dict(J=6, J_fr=2, Q=(8, 2), shape=1024, format='time'), 2),
+    ('joint_j6_jfr2_q82', dict(J=6, J_fr=2, Q=(8, 2), shape=1024, format='joint'), 2),
+    ('time_j5_jfr3_q41_F0_list', dict(J=5, J_fr=3, Q=(4, 1), shape=512, F=0, out_type='list', format='time'), 2),
+    ('time_j5_jfr2_q4_global', dict(J=5, J_fr=2, Q=4, shape=512, T='global', F='global', format='time'), 2),
+    ('joint_j5_jfr2_q41_dict', dict(J=5, J_fr=2, Q=(4, 1), shape=512, out_type='dict', format='joint'), 2),
+    ('joint_j4_jfr1_q21_n300', dict(J=4, J_fr=1, Q=(2, 1), shape=300, format='joint'), 3),
+]
+
+
+def jtfs(ref_root):
+    sys.path.insert(0, ref_root)
+    from kymatio.scattering1d.frontend.numpy_frontend import TimeFrequencyScatteringNumPy
+    out, meta = {}, []
+    for i, (name, kw, B) in enumerate(CASES_JTFS):
+        S = TimeFrequencyScatteringNumPy(**kw)
+        x = np.random.default_rng(300 + i).standard_normal((B, kw['shape'])).astype(np.float32)
+        y = S(x.astype(np.float64))
+        out[name + '/x'] = x
+        if isinstance(y, list):
+            for p in y:
+                out[name + '/S/' + ','.join(map(str, p['n']))] = p['coef']
+        elif isinstance(y, dict):
+            for k, v in y.items():
+                out[name + '/S/' + ','.join(map(str, k))] = v
+        else:
+            out[name + '/S'] = y
+        m = S.meta()
+        out[name + '/meta/key'] = np.array(json.dumps([list(map(int, k)) for k in m['key']]))
+        for field in ('order', 'n_fr', 'spin', 'xi_fr', 'sigma_fr', 'j_fr'):
+            out[name + '/meta/' + field] = np.asarray(m[field], dtype=np.float64)
+        meta.append(dict(name=name, kwargs=kw))
+    out['meta'] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, 'ref_jtfs.npz'), **out)
+
+
 if __name__ == '__main__':
     root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
-    main(root)
-    grads(root)
+    what = sys.argv[2:] or ['main', 'grads', 'jtfs']
+    if 'main' in what:
+        main(root)
+    if 'grads' in what:
+        grads(root)
+    if 'jtfs' in what:
+        jtfs(root)
