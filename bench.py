@@ -288,8 +288,28 @@ def _extra_mixed_512(dev, flush, steps, warmup):
             'img_s_graph_tc': 512 / grt * 1e3, 'counts': {str(s): len(v) for s, v in sorted(groups.items())}}
 
 
+def _extra_jtfs_8192(dev, flush, steps, warmup):
+    """Joint time-frequency scattering, N=8192, J=6, J_fr=2, Q=(8,2), batch 64,
+    'time' format (the chirp signals of the 1-D workload), op by op over the
+    CUDA op surface."""
+    import torch
+    from kymatio_gb300.jtfs import TimeFrequencyScattering
+    rng = np.random.default_rng(1)
+    N, B = 8192, 64
+    t = np.arange(N)
+    f0 = rng.uniform(0.01, 0.1, B)[:, None]
+    f1 = rng.uniform(0.1, 0.4, B)[:, None]
+    sig = (rng.standard_normal((B, N)) + np.cos(2 * np.pi * (f0 * t + (f1 - f0) * t ** 2 / (2 * N)))).astype(np.float32)
+    xs = torch.from_numpy(sig).to(dev)
+    S = TimeFrequencyScattering(J=6, J_fr=2, Q=(8, 2), shape=N).to(dev)
+    with torch.no_grad():
+        ms = _time_ms(lambda: S(xs), steps, warmup, flush)
+    return {'sig_s': B / ms * 1e3, 'channels': int(S(xs[:1]).shape[-2])}
+
+
 EXTRAS = {
     'scattering2d_32x32_J2_b128': _extra_s2d_32,
+    'jtfs_8192_J6_Jfr2_Q8_2_b64': _extra_jtfs_8192,
     'scattering1d_8192_J6_Q8_T64_b256': _extra_s1d_8192,
     'scattering2d_128x128_J4_b32_fwd_bwd': _extra_fwd_bwd_128,
     'mixed_512_sides_32_64_128_256': _extra_mixed_512,

@@ -24,7 +24,9 @@ on current scipy) and writes:
 * ``ref_jtfs.npz`` -- seeded inputs and reference numpy FP64 outputs of joint
   time-frequency scattering (formats 'time' and 'joint', out_type array, list
   and dict, F local / zero / global, T global), with each configuration's
-  ``meta()`` (keys, order, n_fr, spin, frequential xi / sigma / j).
+  ``meta()`` (keys, order, n_fr, spin, frequential xi / sigma / j) and, for
+  the array outputs, an upstream gradient and the reference torch frontend's
+  float64 input gradient.
 
 Nothing at test time reads the reference; the tests read these files.
 """
@@ -194,6 +196,16 @@ def jtfs(ref_root):
                 out[name + '/S/' + ','.join(map(str, k))] = v
         else:
             out[name + '/S'] = y
+        if not isinstance(y, (list, dict)):
+            # input gradient through the reference torch frontend's autograd, float64
+            import torch
+            from kymatio.scattering1d.frontend.torch_frontend import TimeFrequencyScatteringTorch
+            St = TimeFrequencyScatteringTorch(**kw).double()
+            xt = torch.from_numpy(x.astype(np.float64)).requires_grad_()
+            yt = St(xt)
+            g = np.random.default_rng(350 + i).standard_normal(tuple(yt.shape)).astype(np.float32)
+            yt.backward(torch.from_numpy(g.astype(np.float64)))
+            out[name + '/g'], out[name + '/gx'] = g, xt.grad.numpy()
         m = S.meta()
         out[name + '/meta/key'] = np.array(json.dumps([list(map(int, k)) for k in m['key']]))
         for field in ('order', 'n_fr', 'spin', 'xi_fr', 'sigma_fr', 'j_fr'):

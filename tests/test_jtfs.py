@@ -168,3 +168,34 @@ def test_jtfs_on_gpu(case):
     S = TimeFrequencyScattering(**_kwargs(case)).to(dev)
     x = torch.from_numpy(_D[case['name'] + '/x']).to(dev)
     _check(case['name'], S(x), 1e-5)
+
+
+GRAD_CASES = [c for c in CASES if c['name'] + '/gx' in _D.files]
+
+
+@pytest.mark.parametrize('case', GRAD_CASES, ids=lambda c: c['name'])
+def test_jtfs_gradient_on_cpu_double(case):
+    """d<g, S(x)>/dx through the restated cascade (torch autograd over the
+    float64 double) against the reference torch frontend's gradient."""
+    from kymatio_gb300.jtfs import TimeFrequencyScattering
+    name = case['name']
+    S = TimeFrequencyScattering(**_kwargs(case))
+    x = torch.from_numpy(_D[name + '/x']).double().requires_grad_()
+    S._jtfs(x, CpuOps).backward(torch.from_numpy(_D[name + '/g']).double())
+    assert rel_l2(x.grad.numpy(), _D[name + '/gx']) <= 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('case', GRAD_CASES, ids=lambda c: c['name'])
+def test_jtfs_gradient_on_gpu(case):
+    """The same gradient through the CUDA ops' adjoints (FFTs, wavelet
+    products, periodisation, modulus, reflect padding)."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from kymatio_gb300.jtfs import TimeFrequencyScattering
+    dev = torch.device('cuda:0')
+    name = case['name']
+    S = TimeFrequencyScattering(**_kwargs(case)).to(dev)
+    x = torch.from_numpy(_D[name + '/x']).to(dev).requires_grad_()
+    S(x).backward(torch.from_numpy(_D[name + '/g']).to(dev))
+    assert rel_l2(x.grad.cpu().numpy(), _D[name + '/gx']) <= 1e-5
