@@ -1117,8 +1117,14 @@ static int run_backward_saved(CascadePlan* P, const void* saved, size_t saved_si
                       static_cast<const float2*>(saved));
 }
 
+// Images per chunk: as many as keep the chunk's parent spectra within 512 MiB.
+// Large launches keep every SM busy through the tail of each group; the
+// parents spill from L2 to HBM, but the children of a parent are adjacent
+// tasks that run in the same wave and read it from L2, so HBM sees each
+// parent about once per group (measured at 256x256 J=3, batch 64: the whole
+// batch in one chunk runs 2.49 ms against 2.82 ms with 64 MiB chunks).
 static void set_default_chunk(CascadePlan* P) {
-  const double budget = 64.0 * 1024 * 1024;  // keep parent spectra L2-resident
+  const double budget = 512.0 * 1024 * 1024;
   long long c = P->u1_elems ? (long long)(budget / (P->u1_elems * sizeof(float2))) : 1 << 20;
   P->chunk = (int)std::max<long long>(1, std::min<long long>(c, 1 << 20));
 }
