@@ -345,7 +345,16 @@ def run_ours(args, world, rank, local):
     chunk = lib.kym_s2d_get_chunk(plan.h)
     n_chunks = -(-BATCH // min(chunk, BATCH))
     # kernels of the tensor-core form per step: the input stage once, every other group once per chunk
-    launches_per_step = sum(gi[7] * (1 if gi[0] == 0 else n_chunks) for gi in ginfo)
+    imgs_chunk = -(-BATCH // n_chunks)
+
+    def sub_launches(gi, imgs):
+        # the line-split groups run over as many images as keep their slots within 64 MiB
+        if gi[7] <= 1:
+            return 1
+        step = max(1, (64 << 20) // (gi[1] * gi[2] * gi[3] * 8))
+        return -(-imgs // step)
+    launches_per_step = sum(gi[7] * (sub_launches(gi, BATCH) if gi[0] == 0 else n_chunks * sub_launches(gi, imgs_chunk))
+                            for gi in ginfo)
     out = torch.empty((BATCH, S._channels) + S._out_hw, device=dev)
     ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, BATCH)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)

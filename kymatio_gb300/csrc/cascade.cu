@@ -552,10 +552,17 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
         L.src = a.u1;
         L.src_stride = P->u1_elems;
       }
-      // grid.y is limited to 65535 images per launch
-      for (int i0 = 0; i0 < n; i0 += 65535) {
+      // grid.y is limited to 65535 images per launch.  The line-split passes
+      // round-trip their spectrum slots between passes: they run over as many
+      // images as keep those slots within 64 MiB, so the slots stay in L2.
+      int step = 65535;
+      if (g.lines) {
+        const double slot_bytes = (double)g.tasks.size() * g.L.mr * g.L.mc * sizeof(float2);
+        step = (int)std::max(1.0, std::min(65535.0, 64.0 * 1024 * 1024 / slot_bytes));
+      }
+      for (int i0 = 0; i0 < n; i0 += step) {
         CascadeLaunch Li = L;
-        const int ni = std::min(65535, n - i0);
+        const int ni = std::min(step, n - i0);
         Li.img0 = L.img0 + i0;
         if (Li.src) Li.src = L.src + (size_t)i0 * L.src_stride;
         if (Li.dst) Li.dst = L.dst + (size_t)i0 * L.dst_stride;
