@@ -107,10 +107,11 @@ int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int
 /* Tensor-core form of launch group `group` in kym_s2d_forward_tc: 0 none
  * (FP32 kernel), 1 the low-pass product on tcgen05, 2 the DFT-GEMM form. */
 int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);
-/* Kernel launches that group `group` makes per chunk of images: 1 for a
- * fused cascade kernel, 3 or 4 for the line-split passes of the sizes above
- * one CTA (tensor_cores != 0: in kym_s2d_forward_tc).  No counterpart in the
- * reference (profiling). */
+/* Kernels that group `group` launches per chunk of images: 1 for a fused
+ * cascade kernel; 3 or 4 for the line-split passes of the sizes above one
+ * CTA, per sub-launch (a sub-launch covers as many images as keep the
+ * group's spectrum slots within 64 MiB) (tensor_cores != 0: in
+ * kym_s2d_forward_tc).  No counterpart in the reference (profiling). */
 int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores);
 
 /* Hand-written backward: grad_x (batch, M, N) = (d forward / d x)^T grad_out,
