@@ -20,6 +20,7 @@ import math
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -83,8 +84,7 @@ class ClockSampler:
 
     def start(self):
         try:
-            os.makedirs(os.path.join(ROOT, 'gpurun_out'), exist_ok=True)
-            self.path = os.path.join(ROOT, 'gpurun_out', 'bench_clocks_%d.csv' % os.getpid())
+            self.path = os.path.join(tempfile.gettempdir(), 'kym_bench_clocks_%d.csv' % os.getpid())
             self.f = open(self.path, 'w')
             self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.Q,
                                           '--format=csv,noheader,nounits', '-lms', '200'],
