@@ -78,7 +78,7 @@ def test_cfg1_batch128_vs_fp64_oracle():
 
 
 def test_cfg3_shape_vs_fp64_oracle():
-    """256x256, J=3, L=8 (the padded size 272 runs on a 4-CTA cluster)."""
+    """256x256, J=3, L=8 (the padded size 272 runs as line-split passes)."""
     dev = _cuda()
     from kymatio_gb300 import Scattering2D
     from oracle.scattering2d import Scattering2D as Oracle
@@ -86,6 +86,29 @@ def test_cfg3_shape_vs_fp64_oracle():
     ref = Oracle(3, (256, 256))(x.astype(np.float64))
     out = Scattering2D(3, (256, 256)).to(dev)(torch.from_numpy(x).to(dev)).cpu().numpy()
     _check_orders(out, ref, 3, 8, 2)
+
+
+def test_line_split_sub_launches():
+    """256x256, J=3 with 16 images: the line-split 272x272 passes run in two
+    sub-launches (as many images as keep their slots within 64 MiB of L2,
+    then the rest).  The last image, in the second sub-launch, matches the
+    FP64 oracle in both forms, and the batch equals the same images run one
+    at a time."""
+    dev = _cuda()
+    from kymatio_gb300 import Scattering2D
+    from oracle.scattering2d import Scattering2D as Oracle
+    x = np.random.default_rng(16).random((16, 256, 256)).astype(np.float32)
+    ref = Oracle(3, (256, 256))(x[[0, 15]].astype(np.float64))
+    S = Scattering2D(3, (256, 256)).to(dev)
+    xd = torch.from_numpy(x).to(dev)
+    out = S(xd)
+    _check_orders(out[[0, 15]].cpu().numpy(), ref, 3, 8, 2)
+    S.set_chunk(1)
+    assert torch.equal(out, S(xd))
+    S.set_chunk(16)
+    S.tensor_cores = True
+    _check_orders(S(xd)[[0, 15]].cpu().numpy(), ref, 3, 8, 2, tol=5e-5)
+    assert S.tensor_core_status() == 0
 
 
 def test_chunking_is_invisible():
