@@ -8,9 +8,11 @@ forward over the batch.  Inputs are generated synthetically (no dataset).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --extra NAME      # one of the other workloads alone (profiling)
 
---impl reference times the reference algorithm's CPU implementation (the
-numpy oracle port of kymatio's numpy backend, float32 arithmetic like the
-reference's fp32 path) on the host cores, on a bounded sample per step.
+--impl reference times the reference's own CPU implementation of the path:
+kymatio's stock ``ScatteringTorch2D`` (torch on the host cores, float32, all
+host threads), pip-installed from the reference into baseline/_ref, on the
+full 64-image batch per step.  Where that install is missing it falls back to
+the oracle port of kymatio's numpy backend (``kind: "port"``).
 Under torchrun each rank is an independent replica (images shard with no
 exchange step): value = images over all ranks / max time over ranks.
 """
@@ -56,6 +58,50 @@ def algorithmic_bytes_per_image(J=J, L=L, side=SIDE):
     out = 4 * C * (side // 2 ** J) ** 2
     spill = 2 * 8 * L * sum((Mp // 2 ** j1) ** 2 for j1 in range(J - 1))
     return 4 * side * side + out + spill
+
+
+def group_fft_flops(level, ntasks, rows, cols, s_out):
+    """5 n log2 n FLOPs per image of one launch group of the reference
+    algorithm: the input stage does the FFT2 of the padded image and the
+    small IFFT2 of S0; every path of an order-1 or order-2 group does the
+    IFFT2 and the FFT2 at its resolution and the small IFFT2 of its output."""
+    f2 = lambda m, n: 5.0 * m * n * math.log2(m * n)
+    if level == 0:
+        return f2(rows, cols) + f2(s_out, s_out)
+    return ntasks * (2 * f2(rows, cols) + f2(s_out, s_out))
+
+
+def s1d_algorithmic(mod):
+    """(bytes, FLOPs) per signal of the 1-D local-averaging cascade
+    (kymatio/scattering1d/core/scattering1d.py:40-107): input, output and one
+    write + read of every first-order spectrum that has children; 5 n log2 n
+    per FFT of the reference algorithm."""
+    f = lambda n: 5.0 * n * math.log2(n) if n > 1 else 0.0
+    n_pad, l2s = mod._N_padded, mod.log2_stride
+    n_out = n_pad >> l2s
+    j1s = [p['j'] for p in mod.psi1_f]
+    j2s = [p['j'] for p in mod.psi2_f] if mod.max_order >= 2 else []
+    flops = f(n_pad) + f(n_out)
+    spill = 0
+    for a in j1s:
+        k1 = min(a, l2s)
+        n1 = n_pad >> k1
+        flops += 2 * f(n1) + f(n_out)
+        kids = [b for b in j2s if b > a]
+        if kids:
+            spill += 2 * 8 * n1
+        for b in kids:
+            k2 = max(min(b, l2s) - k1, 0)
+            flops += 2 * f(n1 >> k2) + f(n_out)
+    C = len(mod._paths())
+    return 4 * mod.shape[0] + 4 * C * n_out + spill, flops
+
+
+def fp32_peak_tflops(dev, mhz):
+    """FP32 pipe peak derived from the device: SMs x 128 FP32 lanes x 2 (FMA)
+    x SM clock (the median sampled under load)."""
+    import torch
+    return torch.cuda.get_device_properties(dev).multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
 
 
 def fft_flops_per_image(J=J, L=L, side=SIDE):
@@ -117,21 +163,96 @@ class ClockSampler:
                 'reasons': reasons, 'samples': len(rows)}
 
 
-def cpu_reference_rate(n_img, threads, repeats=1):
-    """Time the reference algorithm (oracle port, float32 like the reference's
-    fp32 numpy path) on n_img images; returns (img/s, seconds)."""
+_REF = {}
+
+
+def reference_kymatio():
+    """The reference package as pip-installed into baseline/_ref (its stock
+    frontends, backends and filter banks), or None when it is not there."""
+    if 'mod' in _REF:
+        return _REF['mod']
+    path = os.path.join(ROOT, 'baseline', '_ref')
+    mod = None
+    if os.path.isfile(os.path.join(path, 'kymatio', '__init__.py')):
+        dont = sys.dont_write_bytecode
+        sys.dont_write_bytecode = True
+        sys.path.insert(0, path)
+        try:
+            import kymatio
+            # the frontend modules directly: kymatio.torch also imports the
+            # 3-D filter bank, whose scipy import fails on current scipy
+            from kymatio.scattering1d.frontend import torch_frontend as _f1  # noqa: F401
+            from kymatio.scattering2d.frontend import numpy_frontend as _n2  # noqa: F401
+            from kymatio.scattering2d.frontend import torch_frontend as _f2  # noqa: F401
+            mod = kymatio
+        except Exception:
+            mod = None
+        finally:
+            sys.path.remove(path)
+            sys.dont_write_bytecode = dont
+    _REF['mod'] = mod
+    return mod
+
+
+def _best_s(fn, repeats, warm=True):
+    if warm:
+        fn()
+    best = float('inf')
+    for _ in range(repeats):
+        t = time.perf_counter()
+        fn()
+        best = min(best, time.perf_counter() - t)
+    return best
+
+
+def ref_torch_module(J_, shape, **kw):
+    """The reference's stock torch frontend (CPU), built once per geometry."""
+    key = ('t2d', J_, tuple(shape) if not isinstance(shape, int) else shape, tuple(sorted(kw.items())))
+    if key not in _REF:
+        kym = reference_kymatio()
+        if isinstance(shape, int):
+            from kymatio.scattering1d.frontend.torch_frontend import ScatteringTorch1D
+            _REF[key] = ScatteringTorch1D(J_, shape, **kw)
+        else:
+            from kymatio.scattering2d.frontend.torch_frontend import ScatteringTorch2D
+            _REF[key] = ScatteringTorch2D(J_, shape, **kw)
+        assert kym is not None
+    return _REF[key]
+
+
+def cpu_reference_rate(n_img, threads, repeats=1, x=None):
+    """Images/s of the reference's CPU implementation on n_img images of the
+    workload (best of ``repeats`` after one warm-up): kymatio's stock
+    ScatteringTorch2D in float32 on ``threads`` host threads when the
+    reference is installed (kind "reference"), else the oracle port of its
+    numpy backend in float32 (kind "port").  Returns (img/s, seconds, kind)."""
+    import torch
+    if x is None:
+        x = grf_batch(n_img, seed=2)
+    if reference_kymatio() is not None:
+        torch.set_num_threads(threads)
+        S = ref_torch_module(J, (SIDE, SIDE), L=L)
+        xt = torch.from_numpy(x[:n_img])
+        with torch.no_grad():
+            best = _best_s(lambda: S(xt), repeats)
+        return n_img / best, best, 'reference'
     import scipy.fft
     from oracle.scattering2d import Scattering2D as Oracle
     S = Oracle(J, (SIDE, SIDE), L=L)
-    x = grf_batch(n_img, seed=2)
     with scipy.fft.set_workers(threads):
-        S(x[:1])
-        best = float('inf')
-        for _ in range(repeats):
-            t = time.perf_counter()
-            S(x)
-            best = min(best, time.perf_counter() - t)
-    return n_img / best, best
+        best = _best_s(lambda: S(x[:n_img]), repeats)
+    return n_img / best, best, 'port'
+
+
+def fp64_reference(x):
+    """The FP64 reference output for images x: the reference's numpy frontend
+    fed float64 input (its filters as it builds them), else the oracle port."""
+    kym = reference_kymatio()
+    if kym is not None:
+        from kymatio.scattering2d.frontend.numpy_frontend import ScatteringNumPy2D
+        return ScatteringNumPy2D(J, (x.shape[-2], x.shape[-1]), L=L)(x.astype(np.float64))
+    from oracle.scattering2d import Scattering2D as Oracle
+    return Oracle(J, (x.shape[-2], x.shape[-1]), L=L)(x.astype(np.float64))
 
 
 def dist_init():
@@ -163,35 +284,58 @@ def barrier(world):
 
 
 def run_reference(args, world, rank):
+    """The reference's own CPU implementation on the host cores: one step is
+    one forward of kymatio's stock ScatteringTorch2D over the full batch."""
     if rank != 0:
         return
+    import torch
     threads = os.cpu_count() or 1
-    n = 4
-    # warm-up steps then timed steps, each a bounded sample of the workload
+    torch.set_num_threads(threads)
+    x = grf_batch(BATCH, seed=2)
+    kind = 'reference' if reference_kymatio() is not None else 'port'
+    if kind == 'reference':
+        S = ref_torch_module(J, (SIDE, SIDE), L=L)
+        xt = torch.from_numpy(x)
+
+        def step():
+            with torch.no_grad():
+                S(xt)
+        what = ("kymatio's stock ScatteringTorch2D (torch %s on the CPU, fp32, %d threads), the full %d-image "
+                'batch per step' % (torch.__version__, threads, BATCH))
+    else:
+        import scipy.fft
+        from oracle.scattering2d import Scattering2D as Oracle
+        So = Oracle(J, (SIDE, SIDE), L=L)
+
+        def step():
+            with scipy.fft.set_workers(threads):
+                So(x)
+        what = ('reference not installed in baseline/_ref: oracle port of its numpy backend, fp32, '
+                'scipy.fft workers=%d, the full %d-image batch per step' % (threads, BATCH))
     for _ in range(args.warmup):
-        cpu_reference_rate(1, threads)
+        step()
     times = []
     for _ in range(args.steps):
-        rate, sec = cpu_reference_rate(n, threads)
-        times.append(sec)
-    value = n * len(times) / sum(times)
+        t = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t)
+    value = BATCH * len(times) / sum(times)
     line = {'metric': METRIC, 'value': value, 'unit': 'img/s', 'n_gpus': args.gpus, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': 1e3 * sum(times) / len(times), 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
             'impl': 'reference',
-            'config': {'workload': 'Scattering2D J=3 L=8 max_order=2 256x256 GRF, %d-image sample per step' % n,
-                       'global_batch': BATCH, 'parallelism': 'host cores'},
-            'cpu_baseline': {'value': value, 'unit': 'img/s', 'cores': threads, 'kind': 'port',
-                             'sample': '%d images per step, oracle port of the reference numpy backend, '
-                                       'fp32, scipy.fft workers=%d' % (n, threads)},
+            'config': {'workload': 'Scattering2D J=3 L=8 max_order=2, 256x256 GRF float32',
+                       'global_batch': BATCH, 'per_gpu_batch': BATCH, 'parallelism': 'host cores'},
+            'cpu_baseline': {'value': value, 'unit': 'img/s', 'cores': threads, 'kind': kind, 'sample': what},
             'e2e': {'value': value, 'unit': 'img/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
 
 
 def order_rel_l2(out, ref):
-    from oracle.scattering2d import order_slices
+    """Relative L2 error per scattering order (S0, S1, S2 channel ranges)."""
+    n1 = J * L
     res = []
-    for sl in order_slices(J, L, 2):
+    for sl in (slice(0, 1), slice(1, 1 + n1), slice(1 + n1, None)):
         a, b = out[:, sl].astype(np.float64), ref[:, sl]
         res.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
     return res
@@ -214,16 +358,52 @@ def _time_ms(fn, steps, warmup, flush):
     return tot / steps
 
 
+CTX = {'hbm_gbs': 6800.0, 'fp32_tflops': None, 'peak_source': 'fallback', 'cpu': True}
+
+
+def _roofline(bytes_unit, flops_unit, rate, unit):
+    """Both roofline terms of a whole workload at ``rate`` units/s."""
+    r = {'bytes_per_%s' % unit: bytes_unit, 'gflop_per_%s_5nlogn' % unit: flops_unit / 1e9,
+         'hbm': {'achieved_gbs': bytes_unit * rate / 1e9, 'peak_gbs': CTX['hbm_gbs'],
+                 'frac': bytes_unit * rate / 1e9 / CTX['hbm_gbs'], 'peak_source': CTX['peak_source']}}
+    if CTX['fp32_tflops']:
+        r['fp32'] = {'achieved_tflops': flops_unit * rate / 1e12, 'peak_tflops': CTX['fp32_tflops'],
+                     'frac': flops_unit * rate / 1e12 / CTX['fp32_tflops'],
+                     'peak_source': 'derived: SMs x 128 lanes x 2 x median SM clock'}
+    return r
+
+
+def _ref_cpu(fn_build, fn_run, n, unit, repeats=2):
+    """The reference's stock torch frontend on the host cores (all threads,
+    no_grad, best of ``repeats`` after one warm-up): units/s, or None."""
+    if not CTX['cpu'] or reference_kymatio() is None:
+        return None
+    import torch
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    mod = fn_build()
+    with torch.no_grad():
+        sec = _best_s(lambda: fn_run(mod), repeats)
+    return {'value': n / sec, 'unit': unit, 'cores': threads, 'kind': 'reference',
+            'sample': '%d per call, torch %s CPU fp32, best of %d' % (n, torch.__version__, repeats)}
+
+
 def _extra_s2d_32(dev, flush, steps, warmup):
     """32x32, J=2, batch 128, U[0,1) seed 0 (plain and tensor-core forms)."""
     import torch
     from kymatio_gb300 import Scattering2D
-    x = torch.from_numpy(np.random.default_rng(0).random((128, 32, 32)).astype(np.float32)).to(dev)
+    xn = np.random.default_rng(0).random((128, 32, 32)).astype(np.float32)
+    x = torch.from_numpy(xn).to(dev)
     S = Scattering2D(2, (32, 32)).to(dev)
     ms = _time_ms(lambda: S(x), steps, warmup, flush)
     S.tensor_cores = True
     ms_tc = _time_ms(lambda: S(x), steps, warmup, flush)
-    return {'img_s': 128 / ms * 1e3, 'img_s_tc': 128 / ms_tc * 1e3}
+    rate = 128 / ms * 1e3
+    return {'img_s': rate, 'img_s_tc': 128 / ms_tc * 1e3,
+            'roofline_plain': _roofline(algorithmic_bytes_per_image(2, 8, 32), fft_flops_per_image(2, 8, 32),
+                                        rate, 'img'),
+            'cpu_baseline': _ref_cpu(lambda: ref_torch_module(2, (32, 32)),
+                                     lambda m: m(torch.from_numpy(xn)), 128, 'img/s', repeats=3)}
 
 
 def _extra_s1d_8192(dev, flush, steps, warmup):
@@ -236,10 +416,15 @@ def _extra_s1d_8192(dev, flush, steps, warmup):
     f0 = rng.uniform(0.01, 0.1, B)[:, None]
     f1 = rng.uniform(0.1, 0.4, B)[:, None]
     sig = rng.standard_normal((B, N)) + np.cos(2 * np.pi * (f0 * t + (f1 - f0) * t ** 2 / (2 * N)))
-    xs = torch.from_numpy(sig.astype(np.float32)).to(dev)
+    xn = sig.astype(np.float32)
+    xs = torch.from_numpy(xn).to(dev)
     S1 = Scattering1D(6, N, Q=(8, 1), T=64).to(dev)
     ms = _time_ms(lambda: S1(xs), steps, warmup, flush)
-    return {'sig_s': B / ms * 1e3}
+    rate = B / ms * 1e3
+    b, f = s1d_algorithmic(S1)
+    return {'sig_s': rate, 'roofline': _roofline(b, f, rate, 'signal'),
+            'cpu_baseline': _ref_cpu(lambda: ref_torch_module(6, N, Q=(8, 1), T=64),
+                                     lambda m: m(torch.from_numpy(xn)), B, 'signals/s')}
 
 
 def _extra_fwd_bwd_128(dev, flush, steps, warmup):
@@ -260,9 +445,25 @@ def _extra_fwd_bwd_128(dev, flush, steps, warmup):
     fwdbwd = _time_ms(fb, steps, warmup, flush)
     S4.activation_budget = 0  # recompute form: only x kept, spectra and y recomputed
     fwdbwd_rc = _time_ms(fb, steps, warmup, flush)
+    cpu = None
+    if CTX['cpu'] and reference_kymatio() is not None:
+        threads = os.cpu_count() or 1
+        torch.set_num_threads(threads)
+        R = ref_torch_module(4, (128, 128))
+        xc, gc = x4.cpu(), g4.cpu()
+        with torch.no_grad():
+            f_s = _best_s(lambda: R(xc), 2)
+        xq = xc.clone().requires_grad_()
+
+        def rfb():
+            xq.grad = None
+            R(xq).backward(gc)
+        fb_s = _best_s(rfb, 2)
+        cpu = {'fwd_ms': f_s * 1e3, 'fwd_bwd_ms': fb_s * 1e3, 'ratio': fb_s / f_s, 'cores': threads,
+               'kind': 'reference', 'sample': 'the full batch of 32, torch %s CPU autograd, fp32' % torch.__version__}
     return {'fwd_ms': fwd, 'fwd_bwd_ms': fwdbwd, 'ratio': fwdbwd / fwd,
             'policy': 'saved modulus inputs, %.1f MB (4 GiB budget)' % (S4._saved_bytes(32) / 1e6),
-            'fwd_bwd_ms_recompute': fwdbwd_rc, 'ratio_recompute': fwdbwd_rc / fwd}
+            'fwd_bwd_ms_recompute': fwdbwd_rc, 'ratio_recompute': fwdbwd_rc / fwd, 'cpu_baseline': cpu}
 
 
 def _extra_mixed_512(dev, flush, steps, warmup):
@@ -284,8 +485,23 @@ def _extra_mixed_512(dev, flush, steps, warmup):
     gr = _time_ms(lambda: mix.forward_grouped(xs), steps, warmup, flush)
     mixt = MixedScattering2D(list(xs), tensor_cores=True).to(dev)
     grt = _time_ms(lambda: mixt.forward_grouped(xs), steps, warmup, flush)
+    cpu = None
+    if CTX['cpu'] and reference_kymatio() is not None:
+        # one reference module per side (its frontend fixes the shape), on a
+        # sample of 4 images per side, weighted by the batch's counts
+        threads = os.cpu_count() or 1
+        torch.set_num_threads(threads)
+        tot = 0.0
+        for s_, v in sorted(groups.items()):
+            R = ref_torch_module(default_J(s_), (s_, s_))
+            xc = xs[s_][:4].cpu()
+            with torch.no_grad():
+                tot += _best_s(lambda: R(xc), 1) / xc.shape[0] * len(v)
+        cpu = {'value': 512 / tot, 'unit': 'img/s', 'cores': threads, 'kind': 'reference',
+               'sample': '4 images per side, one stock ScatteringTorch2D per side, time scaled to the counts'}
     return {'img_s_per_size_sequential': 512 / seq * 1e3, 'img_s_graph': 512 / gr * 1e3,
-            'img_s_graph_tc': 512 / grt * 1e3, 'counts': {str(s): len(v) for s, v in sorted(groups.items())}}
+            'img_s_graph_tc': 512 / grt * 1e3, 'counts': {str(s): len(v) for s, v in sorted(groups.items())},
+            'cpu_baseline': cpu}
 
 
 def _extra_jtfs_8192(dev, flush, steps, warmup):
@@ -304,7 +520,18 @@ def _extra_jtfs_8192(dev, flush, steps, warmup):
     S = TimeFrequencyScattering(J=6, J_fr=2, Q=(8, 2), shape=N).to(dev)
     with torch.no_grad():
         ms = _time_ms(lambda: S(xs), steps, warmup, flush)
-    return {'sig_s': B / ms * 1e3, 'channels': int(S(xs[:1]).shape[-2])}
+    cpu = None
+    if CTX['cpu'] and reference_kymatio() is not None:
+        from kymatio.scattering1d.frontend.torch_frontend import TimeFrequencyScatteringTorch
+        threads = os.cpu_count() or 1
+        torch.set_num_threads(threads)
+        R = TimeFrequencyScatteringTorch(J=6, J_fr=2, Q=(8, 2), shape=N)
+        xc = torch.from_numpy(sig[:8])
+        with torch.no_grad():
+            sec = _best_s(lambda: R(xc), 1)
+        cpu = {'value': 8 / sec, 'unit': 'signals/s', 'cores': threads, 'kind': 'reference',
+               'sample': '8 signals, stock TimeFrequencyScatteringTorch, torch %s CPU fp32' % torch.__version__}
+    return {'sig_s': B / ms * 1e3, 'channels': int(S(xs[:1]).shape[-2]), 'cpu_baseline': cpu}
 
 
 EXTRAS = {
@@ -401,14 +628,22 @@ def run_ours(args, world, rank, local):
             gtot += np.array([gms[i] for i in range(ngroups)])
         return max_over_ranks(sum(times) / len(times), world), gtot / args.steps
 
-    # precision of each form on two images vs the FP64 oracle
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except Exception:
+        pass
+    CTX['hbm_gbs'] = peaks.get('hbm_gbs', 6800.0)
+    CTX['peak_source'] = 'measured' if 'hbm_gbs' in peaks else 'fallback'
+    CTX['cpu'] = not args.no_cpu
+    # precision of each form on two images vs the FP64 reference (the
+    # reference's numpy frontend fed float64)
     prec = {}
     if rank == 0 and not args.no_cpu:
-        from oracle.scattering2d import Scattering2D as Oracle
         # the first and the last image: the last one sits in the last chunk and
         # the last sub-launch of the line-split groups
         pick = [0, BATCH - 1] if BATCH > 1 else [0]
-        ref = Oracle(J, (SIDE, SIDE), L=L)(x_np[pick].astype(np.float64))
+        ref = fp64_reference(x_np[pick])
         for form in ('plain', 'tc', 'tc_dft'):
             prev = lib.kym_set_tc_dft(1 if form == 'tc_dft' else 0)
             step('plain' if form == 'plain' else 'tc', False)
@@ -471,13 +706,12 @@ def run_ours(args, world, rank, local):
         bytes_launch = imgs_per_launch * (n_src * 8 * src + ntasks * 4 * side_out ** 2 + spill_w) + \
             ntasks * (4 * src + 4 * rows * cols)
     dur_s = per_launch[dom] / 1e3
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
-    except Exception:
-        pass
-    hbm_peak = peaks.get('hbm_gbs', 6800.0)
+    hbm_peak = CTX['hbm_gbs']
     achieved = bytes_launch / dur_s / 1e9
+    s_out = Mp // 2 ** J
+    flops_launch = imgs_per_launch * group_fft_flops(lvl, ntasks, rows, cols, s_out)
+    sm_mhz = (clocks or {}).get('sm_mhz') or peaks.get('sm_max_mhz', 2070.0)
+    CTX['fp32_tflops'] = fp32_peak_tflops(dev, sm_mhz)
     # DRAM bytes of one launch of this group, from the committed ncu summary
     # (null when the dominant group has no capture)
     traffic = None
@@ -490,13 +724,18 @@ def run_ours(args, world, rank, local):
         except Exception:
             traffic = None
     flops_img = fft_flops_per_image()
+    # each form within its bar against the FP64 reference (relative L2 per order)
+    bars = {'plain': 1e-5, 'tc': 5e-5, 'tc_dft': 5e-5}
+    prec_ok = None if not prec else all(max(v) <= bars[k] for k, v in prec.items())
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, sec = cpu_reference_rate(8, threads)
-        cpu = {'value': rate, 'unit': 'img/s', 'cores': threads, 'kind': 'port',
-               'sample': '8 GRF images (%.1f s), oracle port of the reference numpy backend in fp32, '
-                         'scipy.fft workers=%d' % (sec, threads)}
+        rate, sec, kind = cpu_reference_rate(BATCH, threads, repeats=1, x=x_np)
+        cpu = {'value': rate, 'unit': 'img/s', 'cores': threads, 'kind': kind,
+               'sample': ('the full %d-image batch (%.1f s after one warm-up), ' % (BATCH, sec)) +
+                         ("kymatio's stock ScatteringTorch2D, torch CPU fp32, %d threads" % threads
+                          if kind == 'reference' else
+                          'oracle port of the reference numpy backend in fp32, scipy.fft workers=%d' % threads)}
     extra = None
     if rank == 0 and world == 1 and not args.no_extras:
         extra = extras(dev, flush)
@@ -526,6 +765,13 @@ def run_ours(args, world, rank, local):
             'gpu_launches': launches_per_step * args.steps,
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s',
                          'frac': achieved / hbm_peak, 'traffic': traffic,
+                         'fp32': {'achieved_tflops': flops_launch / dur_s / 1e12,
+                                  'peak_tflops': CTX['fp32_tflops'],
+                                  'frac': flops_launch / dur_s / 1e12 / CTX['fp32_tflops'],
+                                  'flops': '5 n log2 n per FFT of the reference algorithm',
+                                  'peak_source': 'derived: SMs x 128 lanes x 2 x median SM clock %.0f MHz'
+                                                 % sm_mhz},
+                         'step': _roofline(algorithmic_bytes_per_image(), flops_img, value / world, 'img'),
                          'kernel': 'cascade group %d (level %d, %dx%d, fold %d, %d tasks%s)'
                                    % (dom, lvl, rows, cols, fold, ntasks,
                                       ', tensor-core' if uses_tc else
@@ -534,12 +780,16 @@ def run_ours(args, world, rank, local):
                          'peak_source': 'measured' if 'hbm_gbs' in peaks else 'fallback'},
             'fp32_fft': {'gflop_per_img_5nlogn': flops_img / 1e9,
                          'achieved_tflops_plain': flops_img * value_plain / world / 1e12},
+            'precision_ok': prec_ok,
             'group_ms_per_step': [round(v, 4) for v in g_tc],
             'clocks': clocks,
             'cpu_baseline': cpu,
             'extras': extra,
         }
         print(json.dumps(line), flush=True)
+        if prec_ok is False:
+            sys.stderr.write('precision above its bar: %s\n' % json.dumps(prec))
+            sys.exit(3)
 
 
 def main():
@@ -565,6 +815,7 @@ def main():
     if args.extra:
         import torch
         dev = torch.device('cuda', 0)
+        CTX['cpu'] = not args.no_cpu
         flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
         print(json.dumps({'extra': args.extra, **extras(dev, flush, args.steps, args.warmup, [args.extra])[args.extra]}))
         return

@@ -6,8 +6,8 @@ group's fused cascade on its own CUDA stream.  The whole batch is captured
 once into a single CUDA graph (fork/join over the streams); later batches
 with the same composition replay it with one host launch, the size groups
 running concurrently on the GPU.  An autotuner (``autotune``) picks each
-group's parent-spectrum chunk, kernel family and precision form by timing
-candidates, and caches the choice per (N, J, L, form) in a JSON file.
+size's parent-spectrum chunk (images per order-2 pass) by timing candidates,
+and caches the choice per (N, J, L, form, batch bucket) in a JSON file.
 """
 import json
 import math
@@ -131,8 +131,12 @@ class MixedScattering2D(torch.nn.Module):
             cur.wait_stream(st)
         return outs
 
-    def forward_grouped(self, xs):
-        """xs: {side: (B_s, side, side) tensor} -> {side: output}, one graph launch."""
+    def forward_grouped(self, xs, copy=True):
+        """xs: {side: (B_s, side, side) tensor} -> {side: output}, one graph launch.
+
+        With ``copy=False`` the returned tensors are the graph's own output
+        buffers: the next call with the same composition overwrites them.
+        By default they are copied out first."""
         key = tuple(sorted((s, tuple(x.shape)) for s, x in xs.items()))
         dev = next(iter(xs.values())).device
         if self.tune:
@@ -140,7 +144,7 @@ class MixedScattering2D(torch.nn.Module):
                 autotune(self.mods[str(s)], x.shape[0])
         if not self.graph:
             streams = [torch.cuda.Stream(dev) for _ in xs]
-            return self._run_groups(xs, streams)
+            return self._run_groups(xs, streams)  # fresh outputs every call
         if key not in self._graphs:
             static_in = {s: x.clone() for s, x in xs.items()}
             streams = [torch.cuda.Stream(dev) for _ in xs]
@@ -157,7 +161,9 @@ class MixedScattering2D(torch.nn.Module):
         for s, x in xs.items():
             static_in[s].copy_(x)
         g.replay()
-        return static_out
+        if not copy:
+            return static_out
+        return {s: o.clone() for s, o in static_out.items()}
 
     def forward(self, images):
         idx = self._groups(images)

@@ -366,12 +366,8 @@ template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT>
 cudaError_t ct_bwd_launch(const BwdLaunch& L, const FilterTable& F, int nimg, cudaStream_t stream) {
   using E = CtEngine<MR, MC, SR, SC, C, ONED, NT>;
   auto kern = ct_bwd_kernel<MR, MC, SR, SC, C, ONED, NT>;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E::smem);
-    if (err != cudaSuccess) return err;
-    configured = true;
-  }
+  static SmemOptin optin;
+  if (cudaError_t err = optin.ensure(kern, (int)E::smem); err != cudaSuccess) return err;
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(L.ntasks * C, nimg, 1);

@@ -284,8 +284,12 @@ struct CascadePlan {
   long long gy1_elems = 0, gy2_elems = 0;  // per image: order-1 / order-2 gradient blocks (complex)
   int bchunk = 0;
   TwiddleBank tw;
-  std::mutex mu;                     // guards `dev`
+  std::mutex mu;                     // guards `dev` and `scratch_tables`
   std::map<int, DeviceState> dev;    // task and twiddle tables, per device
+  // host image of the task and twiddle tables as the allocation-free forward
+  // lays them out at the head of its scratch array; built on its first call
+  // and kept for the plan's lifetime, so a copy from it never outlives it
+  std::vector<unsigned char> scratch_tables;
   ~CascadePlan() {
     int cur = 0;
     const bool have = cudaGetDevice(&cur) == cudaSuccess;
@@ -322,6 +326,10 @@ static int finalize_groups(CascadePlan* P) {
     }
   }
   P->u1_elems += lp;
+  // per-image strides stay even (16-byte aligned complex64 pairs): bulk copies
+  // of source rows read from them
+  P->u0_elems += P->u0_elems & 1;
+  P->u1_elems += P->u1_elems & 1;
   P->all_tasks.clear();
   for (auto& g : P->groups) P->all_tasks.insert(P->all_tasks.end(), g.tasks.begin(), g.tasks.end());
   return KYM_OK;
@@ -429,15 +437,8 @@ template <bool CL, bool ONED>
 static cudaError_t launch_group(const Group& g, const CascadeLaunch& L, const FilterTable& F, int nimg,
                                 cudaStream_t stream) {
   auto kern = cascade_kernel<CL, ONED>;
-  static int configured_device = -1;  // opt into the largest dynamic smem once per device
-  int d = 0;
-  cudaGetDevice(&d);
-  if (configured_device != d) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)max_dynamic_smem());
-    if (e != cudaSuccess) return e;
-    configured_device = d;
-  }
+  static SmemOptin optin;  // the largest dynamic shared memory, once per device
+  if (cudaError_t e = optin.ensure(kern, (int)max_dynamic_smem()); e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(L.ntasks * L.cluster, nimg, 1);
@@ -665,7 +666,10 @@ static void attach_tc(CascadePlan* P) {
       // the DFT-GEMM fold pass reads its paths as a P x 8 grid: path p * 8 + q
       // folds source p with wavelet q (sources and wavelets shared along rows
       // and columns), from 16-byte-aligned rows
-      bool grid = (g.tasks.size() == 8 || g.tasks.size() == 64) && (P->u0_elems % 2 == 0);
+      // the stride the fold reads per image: the input spectra for order 1,
+      // the parent spectra for order 2
+      const long long src_stride = g.level == 1 ? P->u0_elems : P->u1_elems;
+      bool grid = (g.tasks.size() == 8 || g.tasks.size() == 64) && (src_stride % 2 == 0);
       for (size_t i = 0; grid && i < g.tasks.size(); ++i) {
         const Task& t = g.tasks[i];
         grid = t.src_off % 2 == 0 && t.src_off == g.tasks[i / 8 * 8].src_off && t.psi == g.tasks[i % 8].psi &&
@@ -710,11 +714,19 @@ int run_plan_in_scratch(CascadePlan* P, const float* x, float* out, int batch, c
     return KYM_ERR_WORKSPACE;
   }
   unsigned char* base = static_cast<unsigned char*>(scratch);
-  // tables: copied on the stream, so earlier calls on the same stream finish first
-  std::vector<unsigned char> img(tables, 0);
-  if (nt) std::memcpy(img.data(), P->all_tasks.data(), nt * sizeof(Task));
-  if (nw) std::memcpy(img.data() + tasks_bytes, P->tw.host().data(), nw * sizeof(float2));
-  cudaError_t e = cudaMemcpyAsync(base, img.data(), tables, cudaMemcpyHostToDevice, stream);
+  // tables: copied on the stream, so earlier calls on the same stream finish
+  // first.  The host image belongs to the plan (immutable once built).
+  const unsigned char* img = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(P->mu);
+    if (P->scratch_tables.size() != tables) {
+      P->scratch_tables.assign(tables, 0);
+      if (nt) std::memcpy(P->scratch_tables.data(), P->all_tasks.data(), nt * sizeof(Task));
+      if (nw) std::memcpy(P->scratch_tables.data() + tasks_bytes, P->tw.host().data(), nw * sizeof(float2));
+    }
+    img = P->scratch_tables.data();
+  }
+  cudaError_t e = cudaMemcpyAsync(base, img, tables, cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) return fail_cuda(e, "scratch table copy");
   DeviceState ds;
   ds.tasks = reinterpret_cast<Task*>(base);
@@ -726,8 +738,6 @@ int run_plan_in_scratch(CascadePlan* P, const float* x, float* out, int batch, c
   a.u0 = reinterpret_cast<float2*>(base + tables);
   a.u1 = a.u0 + (size_t)a.chunk * P->u0_elems;
   a.stage0_per_chunk = true;
-  // a copy from pageable memory returns once the host image is staged, so
-  // `img` may go out of scope before the transfer completes
   return run_core(P, x, out, batch, F, a, stream);
 }
 
@@ -896,15 +906,8 @@ template <bool CL, bool ONED>
 static cudaError_t launch_rt_bwd(const BwdGroup& b, const BwdLaunch& L, const FilterTable& F, int nimg,
                                  cudaStream_t stream) {
   auto kern = rt_bwd_kernel<CL, ONED>;
-  static int configured_device = -1;
-  int d = 0;
-  cudaGetDevice(&d);
-  if (configured_device != d) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)max_dynamic_smem());
-    if (e != cudaSuccess) return e;
-    configured_device = d;
-  }
+  static SmemOptin optin;  // the largest dynamic shared memory, once per device
+  if (cudaError_t e = optin.ensure(kern, (int)max_dynamic_smem()); e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(L.ntasks * L.cluster, nimg, 1);

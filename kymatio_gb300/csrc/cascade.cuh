@@ -13,9 +13,31 @@
 // cascade (kymatio/scattering1d/core/scattering1d.py:40-107) is the same
 // program on a single row.
 #pragma once
+#include <atomic>
+
 #include "fft_engine.cuh"
 
 namespace kym {
+
+// Opt a kernel into a large dynamic shared-memory size on the current device.
+// The attribute is per device, so each call site keeps one of these (static,
+// per kernel instantiation) and sets it once per device ordinal below 64;
+// other ordinals set it on every launch.  Concurrent first calls from several
+// host threads may both set it, which is harmless.
+struct SmemOptin {
+  std::atomic<unsigned long long> done{0};
+  template <class K>
+  cudaError_t ensure(K kern, int bytes) {
+    int d = 0;
+    cudaError_t e = cudaGetDevice(&d);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = (d >= 0 && d < 64) ? (1ull << d) : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_release);
+    return e;
+  }
+};
 
 constexpr int kMaxFilters = 1024;
 

@@ -312,12 +312,8 @@ template <int MR, int MC, int SR, int SC, int C, bool ONED, int NT, int KF>
 cudaError_t ct_launch(const CascadeLaunch& L, const FilterTable& F, int nimg, cudaStream_t stream) {
   using G = CtGeom<MR, MC, SR, SC, C, ONED, NT>;
   auto kern = ct_cascade_kernel<MR, MC, SR, SC, C, ONED, NT, KF>;
-  static bool configured = false;  // per process; attributes are per function
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static SmemOptin optin;
+  if (cudaError_t e = optin.ensure(kern, (int)G::smem); e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(L.ntasks * C, nimg, 1);

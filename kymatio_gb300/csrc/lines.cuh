@@ -261,16 +261,11 @@ cudaError_t lines_launch(const CascadeLaunch& L, const FilterTable& F, int nimg,
   auto k_cols = lines_cols_kernel<MR, MC, NT>;
   auto k_fwd = lines_rows_fwd_kernel<MR, MC, SR, SC, NT>;
   auto k_lp = lines_lowpass_kernel<MR, MC, SR, SC, NT>;
-  static bool configured = false;  // attributes are per function, set once per process
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_in, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::row_smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::col_smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::row_smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static SmemOptin opt_in, opt_cols, opt_fwd;
+  cudaError_t e = opt_in.ensure(k_in, (int)G::row_smem);
+  if (e == cudaSuccess) e = opt_cols.ensure(k_cols, (int)G::col_smem);
+  if (e == cudaSuccess) e = opt_fwd.ensure(k_fwd, (int)G::row_smem);
+  if (e != cudaSuccess) return e;
   k_in<<<dim3(MR / G::RB, L.ntasks, nimg), NT, G::row_smem, stream>>>(L, F);
   k_cols<<<dim3(MC / G::CB, L.ntasks, nimg), NT, G::col_smem, stream>>>(L);
   if (L.modulus) k_fwd<<<dim3(MR / G::RB, L.ntasks, nimg), NT, G::row_smem, stream>>>(L, F);

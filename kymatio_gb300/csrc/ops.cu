@@ -169,14 +169,8 @@ OpPlan* op_plan(int M, int N, int* rc) {
 template <bool CL, bool ONED>
 cudaError_t launch_op_fft(const OpPlan* P, const OpFftLaunch& L, int batch, cudaStream_t stream) {
   auto kern = op_fft2_kernel<CL, ONED>;
-  static int configured = -1;
-  int d = 0;
-  cudaGetDevice(&d);
-  if (configured != d) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_dynamic_smem());
-    if (e != cudaSuccess) return e;
-    configured = d;
-  }
+  static SmemOptin optin;
+  if (cudaError_t e = optin.ensure(kern, (int)max_dynamic_smem()); e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(batch * P->cluster, 1, 1);

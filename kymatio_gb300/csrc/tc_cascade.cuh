@@ -262,12 +262,8 @@ cudaError_t tc_launch(const CascadeLaunch& L, const FilterTable& F, const Lowpas
                       cudaStream_t stream) {
   using G = TcGeom<MR, MC, NOUTC>;
   auto kern = tc_cascade_kernel<MR, MC, NOUTR, NOUTC, KF, NT>;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static SmemOptin optin;
+  if (cudaError_t e = optin.ensure(kern, (int)G::smem); e != cudaSuccess) return e;
   kern<<<dim3(L.ntasks, nimg, 1), NT, G::smem, stream>>>(L, F, LP, status);
   return cudaGetLastError();
 }

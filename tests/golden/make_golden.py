@@ -2,7 +2,7 @@
 
 Run once in a container where the reference checkout is available:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference checkout> [main] [grads] [jtfs]
 
 It imports the reference's numpy frontends (the ``kymatio.numpy`` namespace
 is avoided because it pulls in the 3-D filter bank, whose scipy import fails
@@ -216,7 +216,9 @@ def jtfs(ref_root):
 
 
 if __name__ == '__main__':
-    root = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    if len(sys.argv) < 2:
+        sys.exit('usage: make_golden.py <reference checkout> [main] [grads] [jtfs]')
+    root = sys.argv[1]
     what = sys.argv[2:] or ['main', 'grads', 'jtfs']
     if 'main' in what:
         main(root)

@@ -116,18 +116,22 @@ def test_separable_lowpass_identity(M, J):
 
 def test_reference_frontend_accepts_backend_objects():
     """The reference frontends accept the GB300 backend objects (name check of
-    kymatio/frontend/base_frontend.py:47-50); runs when KYMATIO_REFERENCE
-    points at a reference checkout."""
+    kymatio/frontend/base_frontend.py:47-50); runs when the reference is
+    installed in baseline/_ref or KYMATIO_REFERENCE points at a checkout."""
     import sys
-    ref = os.environ.get('KYMATIO_REFERENCE', '')
-    if not ref or not os.path.isdir(ref):
-        pytest.skip('KYMATIO_REFERENCE not set')
+    cands = [os.environ.get('KYMATIO_REFERENCE', ''), os.path.join(ROOT, 'baseline', '_ref')]
+    ref = next((c for c in cands if c and os.path.isfile(os.path.join(c, 'kymatio', '__init__.py'))), None)
+    if ref is None:
+        pytest.skip('the reference is not installed')
+    dont = sys.dont_write_bytecode
+    sys.dont_write_bytecode = True
     sys.path.insert(0, ref)
     try:
         from kymatio.scattering2d.frontend.torch_frontend import ScatteringTorch2D
         from kymatio.scattering1d.frontend.torch_frontend import ScatteringTorch1D
     finally:
         sys.path.remove(ref)
+        sys.dont_write_bytecode = dont
     from kymatio_gb300.backend import backend1d, backend2d
     S2 = ScatteringTorch2D(2, (32, 32), backend=backend2d)
     assert S2.backend is backend2d

@@ -47,3 +47,19 @@ def test_mixed_batch_tensor_cores():
         s = im.shape[-1]
         ref = Oracle(default_J(s), (s, s))(im.cpu().numpy()[None].astype(np.float64))[0]
         assert rel_l2(o.cpu().numpy(), ref) <= 5e-5
+
+
+def test_mixed_batch_outputs_not_aliased():
+    """Results a caller holds survive the next replay of the same graph."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from kymatio_gb300.batching import MixedScattering2D
+    dev = torch.device('cuda:0')
+    M = MixedScattering2D([32, 64]).to(dev)
+    xs = {32: torch.rand(3, 32, 32, device=dev), 64: torch.rand(2, 64, 64, device=dev)}
+    first = M.forward_grouped(xs)
+    keep = {s: o.clone() for s, o in first.items()}
+    M.forward_grouped({s: torch.rand_like(x) for s, x in xs.items()})
+    torch.cuda.synchronize()
+    for s in xs:
+        assert torch.equal(first[s], keep[s])

@@ -17,13 +17,13 @@ torch = pytest.importorskip('torch')
 pytestmark = pytest.mark.gpu
 
 
-def _setup(J, side, batch, seed):
+def _setup(J, side, batch, seed, L=8):
     if not torch.cuda.is_available():
         pytest.skip('no CUDA device')
     from kymatio_gb300 import Scattering2D, _lib
     lib = _lib.load()
     dev = torch.device('cuda:0')
-    S = Scattering2D(J, (side, side)).to(dev)
+    S = Scattering2D(J, (side, side), L=L).to(dev)
     plan = S._get_plan()
     x = torch.from_numpy(np.random.default_rng(seed).random((batch, side, side)).astype(np.float32)).to(dev)
     return lib, _lib, S, plan, x, dev
@@ -63,6 +63,21 @@ def test_noalloc_matches_forward_twice(J, side, batch):
     x2 = torch.rand_like(x)
     assert rel_l2(_forward_noalloc(lib, _lib, S, plan, x2).cpu().numpy(),
                   _forward_ref(lib, _lib, S, plan, x2).cpu().numpy()) <= 1e-5
+
+
+def test_noalloc_one_image_per_chunk():
+    """320x320, J=3, L=16: one image's input and parent spectra take 19 MB,
+    so the 32 MiB scratch holds a single image and the batch of 3 runs as
+    three chunks of one, each chunk's input stage reusing the same region."""
+    lib, _lib, S, plan, x, dev = _setup(3, 320, 3, seed=23, L=16)
+    per_image = lib.kym_s2d_workspace_bytes(plan.h, 1)
+    assert (16 << 20) < per_image < (31 << 20), per_image
+    ref = _forward_ref(lib, _lib, S, plan, x)
+    for _ in range(2):
+        got = _forward_noalloc(lib, _lib, S, plan, x)
+        torch.cuda.synchronize()
+        assert torch.isfinite(got).all()
+        assert rel_l2(got.cpu().numpy(), ref.cpu().numpy()) <= 1e-5
 
 
 def test_noalloc_rejects_oversized_geometry():
