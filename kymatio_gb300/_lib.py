@@ -28,6 +28,7 @@ SIGNATURES = {
     'kym_last_error': (ctypes.c_char_p, []),
     'kym_set_specialized': (_c_int, [_c_int]),
     'kym_set_tc_dft': (_c_int, [_c_int]),
+    'kym_set_shared_fold': (_c_int, [_c_int]),
     'kym_s2d_plan_create': (_c_int, [_c_int] * 6 + [ctypes.POINTER(_vp)]),
     'kym_s2d_plan_destroy': (_c_int, [_vp]),
     'kym_s2d_plan_info': (_c_int, [_vp] + [_ip] * 6),
@@ -49,6 +50,7 @@ SIGNATURES = {
                                     ctypes.POINTER(_vp), _c_int, _vp, _c_size, _vp, _vp,
                                     ctypes.POINTER(ctypes.c_float), _c_int]),
     'kym_s2d_group_kernels': (_c_int, [_vp, _c_int, _c_int]),
+    'kym_s2d_group_launches': (_c_int, [_vp, _c_int, _c_int, _c_int]),
     'kym_s2d_group_uses_tc': (_c_int, [_vp, _c_int]),
     'kym_tc_selftest': (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _vp, _vp]),
     'kym_s2d_group_count': (_c_int, [_vp]),
