@@ -571,17 +571,10 @@ def run_ours(args, world, rank, local):
                                              lib.kym_s2d_group_kernels(plan.h, g, 1)])
     chunk = lib.kym_s2d_get_chunk(plan.h)
     n_chunks = -(-BATCH // min(chunk, BATCH))
-    # kernels of the tensor-core form per step: the input stage once, every other group once per chunk
-    imgs_chunk = -(-BATCH // n_chunks)
-
-    def sub_launches(gi, imgs):
-        # the line-split groups run over as many images as keep their slots within 64 MiB
-        if gi[7] <= 1:
-            return 1
-        step = max(1, (64 << 20) // (gi[1] * gi[2] * gi[3] * 8))
-        return -(-imgs // step)
-    launches_per_step = sum(gi[7] * (sub_launches(gi, BATCH) if gi[0] == 0 else n_chunks * sub_launches(gi, imgs_chunk))
-                            for gi in ginfo)
+    # kernels of the tensor-core form per step, as the library launches them
+    # (chunks, line-split and shared-fold sub-launches)
+    launches = [lib.kym_s2d_group_launches(plan.h, g, BATCH, 1) for g in range(ngroups)]
+    launches_per_step = sum(launches)
     out = torch.empty((BATCH, S._channels) + S._out_hw, device=dev)
     ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, BATCH)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
@@ -658,6 +651,11 @@ def run_ours(args, world, rank, local):
     prev_dft = lib.kym_set_tc_dft(1)
     t_dft, g_dft = measure('tc')
     lib.kym_set_tc_dft(prev_dft)
+    # both forms with the childless groups in the fused per-path kernels
+    prev_sf = lib.kym_set_shared_fold(0)
+    t_plain_fused, _ = measure('plain')
+    t_tc_fused, g_tc_fused = measure('tc')
+    lib.kym_set_shared_fold(prev_sf)
     clocks = sampler.stop()
     tc_status = S.tensor_core_status()
     value = BATCH * world / (t_tc / 1e3)
@@ -687,6 +685,7 @@ def run_ours(args, world, rank, local):
     e2e_ms = max_over_ranks((e0.elapsed_time(e1) - flush_ms) / args.steps, world)
     e2e = BATCH * world / (e2e_ms / 1e3)
     # ---- roofline of the dominant launch group of the tensor-core form -----------
+    # (one launch = all the kernels of the group over one chunk of images)
     per_launch = [g_tc[g] / (1 if gi[0] == 0 else n_chunks) for g, gi in enumerate(ginfo)]
     dom = int(np.argmax(g_tc))
     lvl, ntasks, rows, cols, fold, cl, uses_tc, nkern = ginfo[dom]
@@ -715,7 +714,8 @@ def run_ours(args, world, rank, local):
     # DRAM bytes of one launch of this group, from the committed ncu summary
     # (null when the dominant group has no capture)
     traffic = None
-    form_key = 'tc' if uses_tc else ('lines' if nkern > 1 else 'fused')
+    sf = nkern > 1 and rows < Mp  # a shared-fold group (line-split passes below the padded size)
+    form_key = 'tc' if uses_tc else ('sf' if sf else ('lines' if nkern > 1 else 'fused'))
     tkey = 'L%d_%dx%d_f%d_%s' % (lvl, rows, cols, fold, form_key)
     tf = os.path.join(ROOT, 'profiles', 'dominant_traffic.json')
     if os.path.exists(tf):
@@ -752,6 +752,11 @@ def run_ours(args, world, rank, local):
                            'rel_l2_vs_fp64': prec.get('plain'),
                            'group_ms_per_step': [round(v, 4) for v in g_plain]},
             'tc_vs_plain': value / value_plain,
+            'fused_per_path': {'plain_img_s': BATCH * world / (t_plain_fused / 1e3),
+                               'tc_img_s': BATCH * world / (t_tc_fused / 1e3),
+                               'tc_group_ms_per_step': [round(v, 4) for v in g_tc_fused],
+                               'what': 'the childless groups in the fused per-path kernels (kym_set_shared_fold(0)) '
+                                       'instead of the shared-fold line-split passes'},
             'tc_dft_gemm': {'value': BATCH * world / (t_dft / 1e3), 'unit': 'img/s', 'ms_per_step': t_dft,
                             'rel_l2_vs_fp64': prec.get('tc_dft'),
                             'group_ms_per_step': [round(v, 4) for v in g_dft],
@@ -775,7 +780,8 @@ def run_ours(args, world, rank, local):
                          'kernel': 'cascade group %d (level %d, %dx%d, fold %d, %d tasks%s)'
                                    % (dom, lvl, rows, cols, fold, ntasks,
                                       ', tensor-core' if uses_tc else
-                                      (', %d line-split kernels' % nkern if nkern > 1 else ', one fused kernel')),
+                                      (', shared-fold rows pass + %d column-side kernels' % (nkern - 1) if sf else
+                                       (', %d line-split kernels' % nkern if nkern > 1 else ', one fused kernel'))),
                          'kernel_ms_per_launch': per_launch[dom],
                          'peak_source': 'measured' if 'hbm_gbs' in peaks else 'fallback'},
             'fp32_fft': {'gflop_per_img_5nlogn': flops_img / 1e9,
