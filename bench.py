@@ -651,11 +651,6 @@ def run_ours(args, world, rank, local):
     prev_dft = lib.kym_set_tc_dft(1)
     t_dft, g_dft = measure('tc')
     lib.kym_set_tc_dft(prev_dft)
-    # both forms with the childless groups in the fused per-path kernels
-    prev_sf = lib.kym_set_shared_fold(0)
-    t_plain_fused, _ = measure('plain')
-    t_tc_fused, g_tc_fused = measure('tc')
-    lib.kym_set_shared_fold(prev_sf)
     clocks = sampler.stop()
     tc_status = S.tensor_core_status()
     value = BATCH * world / (t_tc / 1e3)
@@ -714,8 +709,7 @@ def run_ours(args, world, rank, local):
     # DRAM bytes of one launch of this group, from the committed ncu summary
     # (null when the dominant group has no capture)
     traffic = None
-    sf = nkern > 1 and rows < Mp  # a shared-fold group (line-split passes below the padded size)
-    form_key = 'tc' if uses_tc else ('sf' if sf else ('lines' if nkern > 1 else 'fused'))
+    form_key = 'tc' if uses_tc else ('lines' if nkern > 1 else 'fused')
     tkey = 'L%d_%dx%d_f%d_%s' % (lvl, rows, cols, fold, form_key)
     tf = os.path.join(ROOT, 'profiles', 'dominant_traffic.json')
     if os.path.exists(tf):
@@ -752,11 +746,6 @@ def run_ours(args, world, rank, local):
                            'rel_l2_vs_fp64': prec.get('plain'),
                            'group_ms_per_step': [round(v, 4) for v in g_plain]},
             'tc_vs_plain': value / value_plain,
-            'fused_per_path': {'plain_img_s': BATCH * world / (t_plain_fused / 1e3),
-                               'tc_img_s': BATCH * world / (t_tc_fused / 1e3),
-                               'tc_group_ms_per_step': [round(v, 4) for v in g_tc_fused],
-                               'what': 'the childless groups in the fused per-path kernels (kym_set_shared_fold(0)) '
-                                       'instead of the shared-fold line-split passes'},
             'tc_dft_gemm': {'value': BATCH * world / (t_dft / 1e3), 'unit': 'img/s', 'ms_per_step': t_dft,
                             'rel_l2_vs_fp64': prec.get('tc_dft'),
                             'group_ms_per_step': [round(v, 4) for v in g_dft],
@@ -780,8 +769,7 @@ def run_ours(args, world, rank, local):
                          'kernel': 'cascade group %d (level %d, %dx%d, fold %d, %d tasks%s)'
                                    % (dom, lvl, rows, cols, fold, ntasks,
                                       ', tensor-core' if uses_tc else
-                                      (', shared-fold rows pass + %d column-side kernels' % (nkern - 1) if sf else
-                                       (', %d line-split kernels' % nkern if nkern > 1 else ', one fused kernel'))),
+                                      (', %d line-split kernels' % nkern if nkern > 1 else ', one fused kernel')),
                          'kernel_ms_per_launch': per_launch[dom],
                          'peak_source': 'measured' if 'hbm_gbs' in peaks else 'fallback'},
             'fp32_fft': {'gflop_per_img_5nlogn': flops_img / 1e9,

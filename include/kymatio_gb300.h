@@ -47,18 +47,6 @@ int kym_set_specialized(int enable);
  * reference (a form of kymatio/scattering2d/core/scattering2d.py:48-75). */
 int kym_set_tc_dft(int enable);
 
-/* Run the childless groups whose paths form a sources x wavelets grid (the
- * order-2 groups of a scale pair, and the last order-1 scale) in the
- * shared-fold line-split form when a variant exists and the workspace holds
- * its slots (enable=1, the default): a rows pass folds every source and
- * wavelet row once for the whole group and runs the inverse row FFTs into
- * per-path slots, then column passes finish each path (plain form: the
- * reference's low-pass; kym_s2d_forward_tc: the separable low-pass in FP32).
- * enable=0 runs them in the fused per-path kernels.  Takes effect at the next
- * call.  Returns the previous setting.  No counterpart in the reference (a
- * schedule of kymatio/scattering2d/core/scattering2d.py:55-78). */
-int kym_set_shared_fold(int enable);
-
 /* ------------------------------------------------------------------------
  * 2-D scattering (replaces the forward of ScatteringTorch2D,
  * kymatio/scattering2d/frontend/torch_frontend.py:72-111, driving
@@ -117,18 +105,17 @@ int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int
                        int n_lowpass, void* workspace, size_t workspace_bytes, unsigned* status, void* stream,
                        float* group_ms, int max_groups);
 /* Tensor-core form of launch group `group` in kym_s2d_forward_tc: 0 none
- * (FP32 kernels), 1 the low-pass product on tcgen05, 2 the DFT-GEMM form. */
+ * (FP32 kernel), 1 the low-pass product on tcgen05, 2 the DFT-GEMM form. */
 int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);
 /* Kernels that group `group` launches per chunk of images: 1 for a fused
  * cascade kernel; 3 or 4 for the line-split passes of the sizes above one
- * CTA, or for the shared-fold passes, per sub-launch (a sub-launch covers as
- * many images as keep the group's slots within 64 MiB); 2 for the DFT-GEMM
- * form (tensor_cores != 0: in kym_s2d_forward_tc).  No counterpart in the
- * reference (profiling). */
+ * CTA, per sub-launch (a sub-launch covers as many images as keep the
+ * group's spectrum slots within 64 MiB) (tensor_cores != 0: in
+ * kym_s2d_forward_tc).  No counterpart in the reference (profiling). */
 int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores);
-/* Kernel launches of group `group` in one forward over `batch` images, with
- * a workspace of kym_s2d_workspace_bytes(plan, batch).  No counterpart in the
- * reference (profiling). */
+/* Kernel launches of group `group` in one forward over `batch` images (its
+ * chunks and line-split sub-launches; tensor_cores as above).  No
+ * counterpart in the reference (profiling). */
 int kym_s2d_group_launches(const kym_s2d_plan* plan, int group, int batch, int tensor_cores);
 
 /* Hand-written backward: grad_x (batch, M, N) = (d forward / d x)^T grad_out,

@@ -28,7 +28,6 @@ SIGNATURES = {
     'kym_last_error': (ctypes.c_char_p, []),
     'kym_set_specialized': (_c_int, [_c_int]),
     'kym_set_tc_dft': (_c_int, [_c_int]),
-    'kym_set_shared_fold': (_c_int, [_c_int]),
     'kym_s2d_plan_create': (_c_int, [_c_int] * 6 + [ctypes.POINTER(_vp)]),
     'kym_s2d_plan_destroy': (_c_int, [_vp]),
     'kym_s2d_plan_info': (_c_int, [_vp] + [_ip] * 6),

@@ -19,7 +19,6 @@
 #include "bwd.cuh"
 #include "tcdft.cuh"
 #include "lines.cuh"
-#include "o2.cuh"
 #include "plan_util.h"
 #include "errors.h"
 
@@ -231,10 +230,6 @@ struct Group {
   TcLauncher tc = nullptr;
   TcLauncher tcdft = nullptr;     // DFT-GEMM tensor-core variant (childless tasks of the small sizes)
   LinesLauncher lines = nullptr;  // line-split passes (sizes above one CTA, every task owns a slot)
-  O2Launcher o2 = nullptr;        // shared-fold line-split passes (childless P x Q groups, slots in the workspace)
-  size_t o2_task_off = 0;         // the group's tasks with their slot offsets, in the device task array
-  long long o2_img_elems = 0;     // slots (and folded low-pass blocks) of one image, complex elements
-  int o2_step = 0;                // images per sub-launch (their slots stay in L2 between the passes)
   std::vector<Task> tasks;
   size_t task_off = 0;   // offset into the device task array
   size_t smem = 0;
@@ -245,10 +240,6 @@ struct Group {
 int odd_pitch(int n) { return (n % 2 == 0) ? n + 1 : n; }
 std::atomic<bool> g_use_ct{true};
 std::atomic<bool> g_use_tcdft{false};
-std::atomic<bool> g_use_o2{true};
-// slots of one sub-launch of a shared-fold group: within this many bytes, so
-// that they stay in L2 from the rows pass to the column passes
-constexpr double kO2SlotBudget = 64.0 * 1024 * 1024;
 int swz_len(int n) { return n + (n >> 4) + 1; }
 
 }  // namespace
@@ -471,8 +462,6 @@ static cudaError_t launch_group(const Group& g, const CascadeLaunch& L, const Fi
 // runs the input stage chunk by chunk (the workspace then holds the input
 // spectra of one chunk only).
 struct RunArgs {
-  float2* o2ws = nullptr;          // slots of the shared-fold groups (null: those groups run fused)
-  long long o2_cap = 0;            // its size, complex elements
   const LowpassTable* lp = nullptr;  // non-null: tensor-core form for the groups that have one
   unsigned* status = nullptr;
   const DeviceState* ds = nullptr;
@@ -572,21 +561,12 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
         const double slot_bytes = (double)g.tasks.size() * g.L.mr * g.L.mc * sizeof(float2);
         step = (int)std::max(1.0, std::min(65535.0, 64.0 * 1024 * 1024 / slot_bytes));
       }
-      const bool o2 = g.o2 && a.o2ws && !a.ysave && g_use_o2.load() && !(a.lp && g.tcdft && a.opnd) &&
-                      a.o2_cap >= g.o2_img_elems;
-      if (o2) {
-        step = (int)std::min<long long>({(long long)g.o2_step, a.o2_cap / g.o2_img_elems, 65535LL});
-        L.tasks = ds->tasks + g.o2_task_off;
-        L.dst = a.o2ws;
-        L.dst_stride = g.o2_img_elems;
-        L.bsum_off = (long long)g.tasks.size() * g.L.mr * g.L.mc;
-      }
       for (int i0 = 0; i0 < n; i0 += step) {
         CascadeLaunch Li = L;
         const int ni = std::min(step, n - i0);
         Li.img0 = L.img0 + i0;
         if (Li.src) Li.src = L.src + (size_t)i0 * L.src_stride;
-        if (Li.dst && !o2) Li.dst = L.dst + (size_t)i0 * L.dst_stride;  // shared-fold slots: one region
+        if (Li.dst) Li.dst = L.dst + (size_t)i0 * L.dst_stride;
         if (Li.ysave) Li.ysave = L.ysave + (size_t)i0 * L.ysave_stride;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (timed && (int)gi < a.max_groups) {
@@ -595,7 +575,6 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           cudaEventRecord(e0, stream);
         }
         if (a.lp && g.tcdft && a.opnd) err = g.tcdft(Li, F, *a.lp, a.status, ni, stream);
-        else if (o2) err = g.o2(Li, F, a.lp, ni, stream);
         else if (a.lp && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
         else if (g.lines) err = g.lines(Li, F, ni, stream);
         else if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
@@ -629,27 +608,6 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
   return KYM_OK;
 }
 
-// Workspace of a forward over `batch` images: the input spectra of the batch
-// and the parent spectra of one chunk, then the DFT-GEMM operand slots of one
-// chunk (when the plan has such groups), then the slots of one sub-launch of
-// the largest shared-fold group.
-struct WsLayout {
-  size_t spectra, opnd_off, opnd_end, o2_off, o2_end;
-};
-static WsLayout ws_layout(const CascadePlan* P, int batch) {
-  const int chunk = std::max(1, std::min(batch, P->chunk));
-  WsLayout w;
-  w.spectra = ((size_t)batch * P->u0_elems + (size_t)chunk * P->u1_elems) * sizeof(float2);
-  w.opnd_off = (w.spectra + 255) & ~(size_t)255;
-  w.opnd_end = P->opnd_bytes ? w.opnd_off + (size_t)chunk * P->opnd_bytes : w.spectra;
-  long long o2 = 0;
-  for (const Group& g : P->groups)
-    if (g.o2) o2 = std::max(o2, (long long)std::min(g.o2_step, chunk) * g.o2_img_elems);
-  w.o2_off = o2 ? (w.opnd_end + 255) & ~(size_t)255 : w.opnd_end;
-  w.o2_end = w.o2_off + (size_t)o2 * sizeof(float2);
-  return w;
-}
-
 static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
                     int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
                     float* group_ms = nullptr, int max_groups = 0, const LowpassTable* lp = nullptr,
@@ -663,17 +621,14 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   int rc = make_filter_table(P, filters, nfilters, &F);
   if (rc) return rc;
   const int chunk = std::min(batch, P->chunk);
-  const WsLayout W = ws_layout(P, batch);
-  // the fold passes (TMA copies, float4 loads) read sources and wavelets from
-  // 16-byte-aligned bases; the separable low-pass reads its factors as float4
+  const size_t spectra = ((size_t)batch * P->u0_elems + (size_t)chunk * P->u1_elems) * sizeof(float2);
+  // the DFT-GEMM groups of the tensor-core form keep their operand slots after the spectra
+  const size_t opnd_off = (spectra + 255) & ~(size_t)255;
+  // the fold pass copies source and wavelet rows with TMA: 16-byte-aligned bases
   bool aligned = (reinterpret_cast<uintptr_t>(workspace) & 15) == 0;
   for (int i = 0; aligned && i < nfilters; ++i) aligned = (reinterpret_cast<uintptr_t>(filters[i]) & 15) == 0;
-  bool lp_aligned = true;
-  for (int i = 0; lp && i < kMaxLowpass; ++i)
-    lp_aligned = lp_aligned && (reinterpret_cast<uintptr_t>(lp->r[i]) & 15) == 0 &&
-                 (reinterpret_cast<uintptr_t>(lp->c[i]) & 15) == 0;
   const bool dft = lp && !ysave && P->opnd_bytes && g_use_tcdft.load() && aligned;
-  const size_t need = dft ? W.opnd_end : W.spectra;
+  const size_t need = dft ? opnd_off + (size_t)chunk * P->opnd_bytes : spectra;
   if (!workspace || ws_bytes < need) {
     set_error_message("forward", "workspace missing or smaller than the plan requires");
     return KYM_ERR_WORKSPACE;
@@ -690,13 +645,7 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   a.lp = ysave ? nullptr : lp;  // the tensor-core kernels do not save y
   a.status = status;
   a.ysave = ysave;
-  if (dft) a.opnd = static_cast<unsigned char*>(workspace) + W.opnd_off;
-  // the shared-fold groups need their slot region (and aligned operands);
-  // without it they run in the fused kernels
-  if (W.o2_end > W.o2_off && ws_bytes >= W.o2_end && aligned && (!lp || lp_aligned)) {
-    a.o2ws = reinterpret_cast<float2*>(static_cast<unsigned char*>(workspace) + W.o2_off);
-    a.o2_cap = (long long)((W.o2_end - W.o2_off) / sizeof(float2));
-  }
+  if (dft) a.opnd = static_cast<unsigned char*>(workspace) + opnd_off;
   return run_core(P, x, out, batch, F, a, stream);
 }
 
@@ -732,40 +681,6 @@ static void attach_tc(CascadePlan* P) {
         const size_t mp = (size_t)(g.L.mr + 7) / 8 * 8;
         P->opnd_bytes = std::max(P->opnd_bytes, g.tasks.size() * 8 * mp * mp);
       }
-    }
-  }
-}
-
-// Shared-fold line-split variants (o2.cuh) for the childless groups whose
-// tasks form a P x Q grid, task p * Q + q reading source p with wavelet q
-// (order 2: P = Q = L parents and wavelets; order 1: one source, Q = L).
-// Each gets a copy of its tasks with slot offsets in the device task array.
-static void attach_o2(CascadePlan* P) {
-  for (Group& g : P->groups) {
-    g.o2 = nullptr;
-    if (!g_use_ct || P->oned || g.level == 0 || g.L.kr != g.L.kc || g.L.mr != g.L.mc || g.L.sr != g.L.sc) continue;
-    const int n = (int)g.tasks.size();
-    const int Q = P->L, Pn = g.level == 2 ? P->L : 1;
-    if (n != Pn * Q) continue;
-    bool grid = true;
-    for (int i = 0; grid && i < n; ++i) {
-      const Task& t = g.tasks[i];
-      grid = t.dst_off < 0 && t.src_off % 2 == 0 && t.src_off == g.tasks[i / Q * Q].src_off &&
-             t.psi == g.tasks[i % Q].psi && t.phi == g.tasks[0].phi;
-    }
-    const long long src_stride = g.level == 1 ? P->u0_elems : P->u1_elems;
-    if (!grid || src_stride % 2) continue;
-    O2Launcher fn = o2_find(g.L.mr, g.L.kr, Pn, Q, g.L.sr);
-    if (!fn) continue;
-    const long long m2 = (long long)g.L.mr * g.L.mc;
-    g.o2 = fn;
-    g.o2_img_elems = n * (m2 + (long long)g.L.sr * g.L.sc);
-    g.o2_step = (int)std::max(1.0, std::min(65535.0, kO2SlotBudget / (g.o2_img_elems * sizeof(float2))));
-    g.o2_task_off = P->all_tasks.size();
-    for (int i = 0; i < n; ++i) {
-      Task c = g.tasks[i];
-      c.dst_off = i * m2;
-      P->all_tasks.push_back(c);
     }
   }
 }
@@ -1363,7 +1278,6 @@ extern "C" int kym_s2d_plan_create(int M, int N, int J, int L, int max_order, in
   rc = build_backward(P);
   if (rc) goto fail;
   attach_tc(P);
-  attach_o2(P);
   set_default_chunk(P);
   *out = h;
   return KYM_OK;
@@ -1378,10 +1292,6 @@ extern "C" int kym_set_specialized(int enable) {
 
 extern "C" int kym_set_tc_dft(int enable) {
   return kym::g_use_tcdft.exchange(enable != 0) ? 1 : 0;
-}
-
-extern "C" int kym_set_shared_fold(int enable) {
-  return kym::g_use_o2.exchange(enable != 0) ? 1 : 0;
 }
 
 extern "C" int kym_s2d_plan_destroy(kym_s2d_plan* plan) {
@@ -1466,7 +1376,6 @@ extern "C" int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group) {
   if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
   const auto& g = plan->p.groups[group];
   if (g.tcdft && kym::g_use_tcdft.load()) return 2;
-  if (g.o2 && kym::g_use_o2.load()) return 0;  // the shared-fold form's low-pass is FP32
   return g.has_tc ? 1 : 0;
 }
 
@@ -1474,7 +1383,6 @@ extern "C" int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int te
   if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
   const kym::Group& g = plan->p.groups[group];
   if (tensor_cores && g.tcdft && kym::g_use_tcdft.load()) return 2;  // fold pass, GEMM kernel
-  if (g.o2 && kym::g_use_o2.load()) return tensor_cores ? 3 : 4;     // rows, columns, [rows + fold], low-pass
   if (tensor_cores && g.has_tc) return 1;
   if (g.lines) return g.L.modulus ? 4 : 3;  // rows, columns, [rows + fold], low-pass
   return 1;
@@ -1485,17 +1393,16 @@ extern "C" int kym_s2d_group_launches(const kym_s2d_plan* plan, int group, int b
   const CascadePlan& P = plan->p;
   const kym::Group& g = P.groups[group];
   if (batch == 0) return 0;
+  // chunks and line-split sub-launches as run_core forms them
   int chunk = std::max(1, std::min(batch, P.chunk));
   const int nch = (batch + chunk - 1) / chunk;
   chunk = (batch + nch - 1) / nch;
   const int k = kym_s2d_group_kernels(plan, group, tensor_cores);
+  const bool fused_tc = tensor_cores && (g.has_tc || (g.tcdft && kym::g_use_tcdft.load()));
   auto sub = [&](int n) {
-    int step = 65535;
-    if (g.o2 && kym::g_use_o2.load() && !(tensor_cores && g.tcdft && kym::g_use_tcdft.load())) step = g.o2_step;
-    else if (g.lines) {
-      const double slot_bytes = (double)g.tasks.size() * g.L.mr * g.L.mc * sizeof(float2);
-      step = (int)std::max(1.0, std::min(65535.0, 64.0 * 1024 * 1024 / slot_bytes));
-    }
+    if (!g.lines || fused_tc) return 1;
+    const double slot_bytes = (double)g.tasks.size() * g.L.mr * g.L.mc * sizeof(float2);
+    const int step = (int)std::max(1.0, std::min(65535.0, 64.0 * 1024 * 1024 / slot_bytes));
     return (n + step - 1) / step;
   };
   if (g.level == 0) return k * sub(batch);
@@ -1506,8 +1413,11 @@ extern "C" int kym_s2d_group_launches(const kym_s2d_plan* plan, int group, int b
 
 extern "C" size_t kym_s2d_workspace_bytes(const kym_s2d_plan* plan, int batch) {
   if (!plan || batch < 0) return 0;
-  if (batch == 0) return 0;
-  return kym::ws_layout(&plan->p, batch).o2_end;
+  const CascadePlan& P = plan->p;
+  const int chunk = std::min(batch, P.chunk);
+  const size_t spectra = ((size_t)batch * P.u0_elems + (size_t)chunk * P.u1_elems) * sizeof(float2);
+  if (!P.opnd_bytes) return spectra;
+  return ((spectra + 255) & ~(size_t)255) + (size_t)chunk * P.opnd_bytes;
 }
 
 namespace kym {

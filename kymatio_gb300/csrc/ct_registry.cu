@@ -66,33 +66,3 @@ LinesLauncher lines_find(int mr, int mc, int sr, int sc, int kf) {
 }
 
 }  // namespace kym
-
-// ---- order-2 line-split variants with a shared fold (o2.cuh) ------------------
-#include "o2.cuh"
-
-namespace kym {
-
-namespace {
-struct O2Entry {
-  int m, kf, p, q, sr;
-  O2Launcher fn;
-};
-std::vector<O2Entry>& o2_table() {
-  static std::vector<O2Entry> t;
-  return t;
-}
-}  // namespace
-
-void o2_register(int m, int kf, int p, int q, int sr, O2Launcher fn) {
-  std::lock_guard<std::mutex> lock(ct_mutex());
-  o2_table().push_back(O2Entry{m, kf, p, q, sr, fn});
-}
-
-O2Launcher o2_find(int m, int kf, int p, int q, int sr) {
-  std::lock_guard<std::mutex> lock(ct_mutex());
-  for (const O2Entry& e : o2_table())
-    if (e.m == m && e.kf == kf && e.p == p && e.q == q && e.sr == sr) return e.fn;
-  return nullptr;
-}
-
-}  // namespace kym

@@ -28,15 +28,12 @@ constexpr int kLinesPerCta = 16;
 constexpr int kLinesThreads = 256;
 constexpr int kLinesMinBlocks = 3;  // CTAs per SM the register budget is sized for
 
-// RB rows per CTA in the row passes, CB columns per CTA in the column pass
-// (both divide the size; 16 for 272 and 288, 8/17 or 34/17 for the order-2
-// sizes 136 and 68, whose only factors are 2 and 17).
-template <int MR, int MC, int RB_ = kLinesPerCta, int CB_ = kLinesPerCta>
+template <int MR, int MC>
 struct LinesGeom {
-  static constexpr int RB = RB_;                          // rows per CTA (row passes)
-  static constexpr int CB = CB_;                          // columns per CTA (column pass)
-  static constexpr int LDR = MC % 2 == 0 ? MC + 1 : MC;   // odd pitch of a row block
-  static constexpr int LDC = CB % 2 == 0 ? CB + 1 : CB;   // odd pitch of a column block
+  static constexpr int RB = kLinesPerCta;       // rows per CTA (row passes)
+  static constexpr int CB = kLinesPerCta;       // columns per CTA (column pass)
+  static constexpr int LDR = MC + 1;            // odd pitch of a row block
+  static constexpr int LDC = CB + 1;            // odd pitch of a column block
   static constexpr size_t row_smem = (size_t)RB * LDR * sizeof(float2);
   static constexpr size_t col_smem = (size_t)MR * LDC * sizeof(float2);
   static_assert(MR % RB == 0 && MC % CB == 0, "line blocks");
@@ -115,10 +112,10 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
 }
 
 // ---- columns: column transforms (and the modulus) in place in the slot -------
-template <int MR, int MC, int NT, int CB_ = kLinesPerCta>
+template <int MR, int MC, int NT>
 __global__ void __launch_bounds__(NT, kLinesMinBlocks)
     lines_cols_kernel(const __grid_constant__ CascadeLaunch L) {
-  using G = LinesGeom<MR, MC, MR, CB_>;  // the row block size is unused here
+  using G = LinesGeom<MR, MC>;
   constexpr int CB = G::CB, LDC = G::LDC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* A = reinterpret_cast<float2*>(smem_raw);
@@ -156,10 +153,10 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
 // (a residue class of the low-pass fold), so it also forms the complete
 // folded rows p of B = fold_ks(slot * phi) / ks^2 and leaves them at
 // dst + img * dst_stride + bsum_off + task * SR * SC.
-template <int MR, int MC, int SR, int SC, int NT, int RB_ = kLinesPerCta>
+template <int MR, int MC, int SR, int SC, int NT>
 __global__ void __launch_bounds__(NT, kLinesMinBlocks)
     lines_rows_fwd_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
-  using G = LinesGeom<MR, MC, RB_, MC>;  // the column block size is unused here
+  using G = LinesGeom<MR, MC>;
   constexpr int RB = G::RB, LDR = G::LDR;
   constexpr int KSR = MR / SR, KSC = MC / SC, PB = RB / KSR;
   static_assert(RB % KSR == 0 && SR % PB == 0, "row blocks are residue classes of the fold");

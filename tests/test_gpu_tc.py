@@ -36,11 +36,8 @@ def test_tc_split_gemm(M, N, K):
 TOL_TC = 5e-5  # split-precision form, relative L2 per order vs the FP64 oracle
 
 
-@pytest.mark.parametrize('J,side,B,shared', [(3, 256, 2, 0), (3, 256, 2, 1), (2, 32, 16, 1), (4, 128, 4, 1),
-                                             (3, 64, 4, 1), (4, 256, 1, 1)])
-def test_tc_form_vs_fp64_oracle(J, side, B, shared):
-    """shared=0 runs the fused tcgen05 kernels where the shared-fold form
-    would otherwise take a group (256x256 J=3)."""
+@pytest.mark.parametrize('J,side,B', [(3, 256, 2), (2, 32, 16), (4, 128, 4), (3, 64, 4), (4, 256, 1)])
+def test_tc_form_vs_fp64_oracle(J, side, B):
     if not torch.cuda.is_available():
         pytest.skip('no CUDA device')
     from kymatio_gb300 import Scattering2D, _lib
@@ -48,17 +45,12 @@ def test_tc_form_vs_fp64_oracle(J, side, B, shared):
     dev = torch.device('cuda:0')
     x = np.random.default_rng(J * 100 + side).random((B, side, side)).astype(np.float32)
     ref = Oracle(J, (side, side))(x.astype(np.float64))
+    S = Scattering2D(J, (side, side), backend='torch_tc').to(dev)
+    plan = S._get_plan()
     lib = _lib.load()
-    prev = lib.kym_set_shared_fold(shared)
-    try:
-        S = Scattering2D(J, (side, side), backend='torch_tc').to(dev)
-        plan = S._get_plan()
-        used = [lib.kym_s2d_group_uses_tc(plan.h, g) for g in range(lib.kym_s2d_group_count(plan.h))]
-        if not shared:
-            assert any(u >= 1 for u in used), used
-        out = S(torch.from_numpy(x).to(dev)).cpu().numpy()
-    finally:
-        lib.kym_set_shared_fold(prev)
+    used = [lib.kym_s2d_group_uses_tc(plan.h, g) for g in range(lib.kym_s2d_group_count(plan.h))]
+    assert any(u >= 1 for u in used), used
+    out = S(torch.from_numpy(x).to(dev)).cpu().numpy()
     assert S.tensor_core_status() == 0
     for k, sl in enumerate(order_slices(J, 8, 2)):
         e = rel_l2(out[:, sl], ref[:, sl])
