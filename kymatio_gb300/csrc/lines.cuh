@@ -28,6 +28,26 @@ constexpr int kLinesPerCta = 16;
 constexpr int kLinesThreads = 256;
 constexpr int kLinesMinBlocks = 3;  // CTAs per SM the register budget is sized for
 
+// Copy n <= N complex elements from global to shared memory with every load
+// of a thread issued before its first store (N / NT loads in flight per
+// thread): idx(e) gives the global offset, sidx(e) the shared one.
+template <int N, int NT, class GI, class SI>
+__device__ __forceinline__ void staged_copy(float2* __restrict__ dst, const float2* __restrict__ src, int n, GI idx,
+                                            SI sidx) {
+  constexpr int PER = (N + NT - 1) / NT;
+  float2 v[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = threadIdx.x + i * NT;
+    if (e < n) v[i] = src[idx(e)];
+  }
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = threadIdx.x + i * NT;
+    if (e < n) dst[sidx(e)] = v[i];
+  }
+}
+
 template <int MR, int MC>
 struct LinesGeom {
   static constexpr int RB = kLinesPerCta;       // rows per CTA (row passes)
@@ -66,6 +86,30 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
     const float4* src4 = reinterpret_cast<const float4*>(L.src + (size_t)img * L.src_stride + t.src_off);
     const float2* psi2 = reinterpret_cast<const float2*>(F.f[t.psi]);
     const float sc = L.load_scale;
+    if constexpr (KF == 1) {
+      // the product src * psi: every load of a thread in flight before the first use
+      constexpr int PER = (NEL / 2 + NT - 1) / NT;
+      float4 sv[PER];
+      float2 fv[PER];
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < NEL / 2) {
+          const size_t half = ((size_t)r0 * MC >> 1) + e;
+          sv[i] = __ldg(src4 + half);
+          fv[i] = __ldg(psi2 + half);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < NEL / 2) {
+          const int u = (2 * e) / MC, v = (2 * e) % MC;
+          A[u * LDR + v] = make_float2(sv[i].x * fv[i].x * sc, sv[i].y * fv[i].x * sc);
+          A[u * LDR + v + 1] = make_float2(sv[i].z * fv[i].y * sc, sv[i].w * fv[i].y * sc);
+        }
+      }
+    } else
     for (int e = threadIdx.x; e < NEL / 2; e += NT) {
       const int u = (2 * e) / MC, v = (2 * e) % MC;
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -124,22 +168,52 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
   const int c0 = blockIdx.x * CB;
   constexpr int NEL = MR * CB;
   float2* slot = L.dst + (size_t)img * L.dst_stride + t.dst_off + c0;
-  for (int e = threadIdx.x; e < NEL; e += NT) {
-    const int r = e / CB, j = e % CB;
-    A[r * LDC + j] = slot[(size_t)r * MC + j];
-  }
+  staged_copy<NEL, NT>(A, slot, NEL, [](int e) { return (size_t)(e / CB) * MC + e % CB; },
+                       [](int e) { return (e / CB) * LDC + e % CB; });
   __syncthreads();
   const ct::ColLines<LDC> cols{A};
   if (L.modulus) {
     ct::fft_lines<MR, CB, NT>(cols, 0, L.pcol.tw, true);
     float2* ys = (L.ysave && t.y_off >= 0) ? L.ysave + (size_t)img * L.ysave_stride + t.y_off + c0 : nullptr;
-    for (int e = threadIdx.x; e < NEL; e += NT) {
-      const int r = e / CB, j = e % CB;
-      const float2 z = A[r * LDC + j];
-      if (ys) ys[(size_t)r * MC + j] = z;  // saved for the backward
-      A[r * LDC + j] = make_float2(sqrtf(fmaf(z.x, z.x, z.y * z.y)), 0.f);
+    // U = |y| is real: the forward column FFT runs two columns per complex
+    // line, Z = U[:, 2j] + i U[:, 2j+1] in column j (the moduli are held in
+    // registers across the barrier, since column j is overwritten)
+    static_assert(CB % 2 == 0, "column pairs");
+    constexpr int NP = MR * (CB / 2);
+    constexpr int PPT = (NP + NT - 1) / NT;
+    float2 m[PPT];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+      const int e = threadIdx.x + i * NT;
+      if (e < NP) {
+        const int r = e / (CB / 2), j = e % (CB / 2);
+        const float2 z0 = A[r * LDC + 2 * j], z1 = A[r * LDC + 2 * j + 1];
+        if (ys) {  // saved for the backward
+          ys[(size_t)r * MC + 2 * j] = z0;
+          ys[(size_t)r * MC + 2 * j + 1] = z1;
+        }
+        m[i] = make_float2(sqrtf(fmaf(z0.x, z0.x, z0.y * z0.y)), sqrtf(fmaf(z1.x, z1.x, z1.y * z1.y)));
+      }
     }
     __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+      const int e = threadIdx.x + i * NT;
+      if (e < NP) A[(e / (CB / 2)) * LDC + e % (CB / 2)] = m[i];
+    }
+    __syncthreads();
+    ct::fft_lines<MR, CB / 2, NT>(cols, 0, L.pcol.tw, false);
+    // unpack: X_2j[k] = (Z[k] + conj Z[-k]) / 2, X_2j+1[k] = -i (Z[k] - conj Z[-k]) / 2
+    // (exactly Hermitian in k, which the next pass relies on)
+    for (int e = threadIdx.x; e < NP; e += NT) {
+      const int r = e / (CB / 2), j = e % (CB / 2);
+      const float2 a = A[r * LDC + j], b = A[((MR - r) % MR) * LDC + j];
+      const float2 x0 = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+      const float2 x1 = make_float2(0.5f * (a.y + b.y), 0.5f * (b.x - a.x));
+      slot[(size_t)r * MC + 2 * j] = x0;
+      slot[(size_t)r * MC + 2 * j + 1] = x1;
+    }
+    return;
   }
   ct::fft_lines<MR, CB, NT>(cols, 0, L.pcol.tw, false);
   for (int e = threadIdx.x; e < NEL; e += NT) {
@@ -149,52 +223,118 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
 }
 
 // ---- rows2: forward row FFT in place (modulus path), low-pass fold ------------
-// Block b holds the rows p + SR a for p in [b PB, b PB + PB) and a < KSR
-// (a residue class of the low-pass fold), so it also forms the complete
-// folded rows p of B = fold_ks(slot * phi) / ks^2 and leaves them at
+// The low-pass fold sums rows p + SR a (a < KSR): a block holds two such
+// residue classes, so it also forms the complete folded rows of
+// B = fold_ks(slot * phi) / ks^2 for them and leaves them at
 // dst + img * dst_stride + bsum_off + task * SR * SC.
+// The column pass left every column Hermitian (the FFT of the real modulus),
+// so the final spectrum obeys F[MR - r][k] = conj(F[r][(MC - k) % MC]): a
+// block pairs class c with its mirror class SR - c, runs the row FFTs of
+// class c only and writes the mirror rows as conjugate reversals.  Block 0
+// holds the two self-mirrored classes 0 and SR/2 and runs KSR + 1 of their
+// rows.  Grid: SR / 2 blocks per task and image.
+template <int MR, int MC, int SR, int SC>
+struct RowsFwdGeom {
+  static constexpr int KSR = MR / SR, KSC = MC / SC;
+  static constexpr int RB = 2 * KSR;                      // rows per block
+  static constexpr int LDR = MC % 2 == 0 ? MC + 1 : MC;
+  static constexpr size_t smem = (size_t)RB * LDR * sizeof(float2);
+  static constexpr int blocks = SR / 2;
+  static_assert(SR % 2 == 0 && KSR % 2 == 0 && MR % 2 == 0, "mirror classes");
+};
+
+// Local row i of block b: its global row, and (for i >= the computed rows)
+// the local row whose conjugate reversal it is.
+template <int MR, int SR>
+__device__ __forceinline__ void rows_fwd_map(int b, int i, int& grow, int& src, int& ncomp) {
+  constexpr int KSR = MR / SR, H = KSR / 2;
+  if (b > 0) {
+    ncomp = KSR;
+    if (i < KSR) {
+      grow = b + SR * i;
+      src = -1;
+    } else {  // class SR - b, row (SR - b) + SR m mirrors b + SR (KSR - 1 - m)
+      const int m = i - KSR;
+      grow = (SR - b) + SR * m;
+      src = KSR - 1 - m;
+    }
+  } else {
+    // computed: class 0 rows SR a (a <= H), class SR/2 rows SR/2 + SR a (a < H)
+    ncomp = KSR + 1;
+    if (i <= H) {
+      grow = SR * i;
+      src = -1;
+    } else if (i < KSR + 1) {
+      grow = SR / 2 + SR * (i - H - 1);
+      src = -1;
+    } else if (i < KSR + 1 + (H - 1)) {  // class 0, a = H+1 .. KSR-1 mirrors a' = KSR - a
+      const int a = H + 1 + (i - KSR - 1);
+      grow = SR * a;
+      src = KSR - a;
+    } else {  // class SR/2, a = H .. KSR-1 mirrors a' = KSR - 1 - a (local H + 1 + a')
+      const int a = H + (i - KSR - H);
+      grow = SR / 2 + SR * a;
+      src = H + 1 + (KSR - 1 - a);
+    }
+  }
+}
+
 template <int MR, int MC, int SR, int SC, int NT>
 __global__ void __launch_bounds__(NT, kLinesMinBlocks)
     lines_rows_fwd_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
-  using G = LinesGeom<MR, MC>;
-  constexpr int RB = G::RB, LDR = G::LDR;
-  constexpr int KSR = MR / SR, KSC = MC / SC, PB = RB / KSR;
-  static_assert(RB % KSR == 0 && SR % PB == 0, "row blocks are residue classes of the fold");
+  using G = RowsFwdGeom<MR, MC, SR, SC>;
+  constexpr int KSR = G::KSR, KSC = G::KSC, RB = G::RB, LDR = G::LDR;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* A = reinterpret_cast<float2*>(smem_raw);
+  __shared__ int s_grow[RB], s_src[RB];
   const int task = blockIdx.y;
   const Task t = L.tasks[task];
   const int img = blockIdx.z;
-  const int p0 = blockIdx.x * PB;
-  constexpr int NEL = RB * MC;
-  // local row u = pp * KSR + a holds global row p0 + pp + SR * a
-  auto grow = [&](int u) { return p0 + u / KSR + SR * (u % KSR); };
-  float2* slot = L.dst + (size_t)img * L.dst_stride + t.dst_off;
-  for (int e = threadIdx.x; e < NEL; e += NT) {
-    const int u = e / MC, v = e % MC;
-    A[u * LDR + v] = slot[(size_t)grow(u) * MC + v];
+  const int b = blockIdx.x;
+  static_assert(RB <= NT, "one thread per local row for the row map");
+  if (threadIdx.x < RB) {
+    int g, src, nc;
+    rows_fwd_map<MR, SR>(b, threadIdx.x, g, src, nc);
+    s_grow[threadIdx.x] = g;
+    s_src[threadIdx.x] = src;
   }
   __syncthreads();
-  ct::fft_lines<MC, RB, NT>(ct::RowLines<LDR, false>{A}, 0, L.prow.tw, false);
-  for (int e = threadIdx.x; e < NEL; e += NT) {
+  const int ncomp = b > 0 ? KSR : KSR + 1;
+  float2* slot = L.dst + (size_t)img * L.dst_stride + t.dst_off;
+  staged_copy<(KSR + 1) * MC, NT>(A, slot, ncomp * MC, [&](int e) { return (size_t)s_grow[e / MC] * MC + e % MC; },
+                                  [](int e) { return (e / MC) * LDR + e % MC; });
+  __syncthreads();
+  if (b > 0) ct::fft_lines<MC, KSR, NT>(ct::RowLines<LDR, false>{A}, 0, L.prow.tw, false);
+  else ct::fft_lines<MC, KSR + 1, NT>(ct::RowLines<LDR, false>{A}, 0, L.prow.tw, false);
+  // mirror rows: F[i][k] = conj(F[src][(MC - k) % MC])
+  for (int e = threadIdx.x; e < (RB - ncomp) * MC; e += NT) {
+    const int i = ncomp + e / MC, v = e % MC;
+    const float2 z = A[s_src[i] * LDR + (MC - v) % MC];
+    A[i * LDR + v] = make_float2(z.x, -z.y);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < RB * MC; e += NT) {
     const int u = e / MC, v = e % MC;
-    slot[(size_t)grow(u) * MC + v] = A[u * LDR + v];
+    slot[(size_t)s_grow[u] * MC + v] = A[u * LDR + v];
   }
   if (L.skip_s) return;
   const float* phi = F.f[t.phi];
   float2* bsum = L.dst + (size_t)img * L.dst_stride + L.bsum_off + (size_t)task * SR * SC;
-  for (int e = threadIdx.x; e < PB * SC; e += NT) {
-    const int pp = e / SC, q = e % SC;
-    const int p = p0 + pp;
+  // the block's two classes: c0 = b (or 0) and c1 = SR - b (or SR / 2); local
+  // rows of class c, a-th alias: found by global row in s_grow
+  for (int e = threadIdx.x; e < 2 * SC; e += NT) {
+    const int ci = e / SC, q = e % SC;
+    const int p = b > 0 ? (ci ? SR - b : b) : (ci ? SR / 2 : 0);
     float2 acc = make_float2(0.f, 0.f);
+    for (int i = 0; i < RB; ++i) {
+      const int g = s_grow[i];
+      if (g % SR != p) continue;
+      const float2* row = A + i * LDR;
+      const float* frow = phi + (size_t)g * MC;
 #pragma unroll
-    for (int a = 0; a < KSR; ++a) {
-      const float2* row = A + (pp * KSR + a) * LDR;
-      const float* frow = phi + (size_t)(p + SR * a) * MC;
-#pragma unroll
-      for (int b = 0; b < KSC; ++b) {
-        const float2 z = row[q + SC * b];
-        const float f = __ldg(frow + q + SC * b);
+      for (int bb = 0; bb < KSC; ++bb) {
+        const float2 z = row[q + SC * bb];
+        const float f = __ldg(frow + q + SC * bb);
         acc.x = fmaf(z.x, f, acc.x);
         acc.y = fmaf(z.y, f, acc.y);
       }
@@ -259,16 +399,17 @@ cudaError_t lines_launch(const CascadeLaunch& L, const FilterTable& F, int nimg,
   constexpr size_t lp_smem = (size_t)SR * LDB * sizeof(float2);
   auto k_in = lines_rows_in_kernel<MR, MC, NT, KF>;
   auto k_cols = lines_cols_kernel<MR, MC, NT>;
+  using FG = RowsFwdGeom<MR, MC, SR, SC>;
   auto k_fwd = lines_rows_fwd_kernel<MR, MC, SR, SC, NT>;
   auto k_lp = lines_lowpass_kernel<MR, MC, SR, SC, NT>;
   static SmemOptin opt_in, opt_cols, opt_fwd;
   cudaError_t e = opt_in.ensure(k_in, (int)G::row_smem);
   if (e == cudaSuccess) e = opt_cols.ensure(k_cols, (int)G::col_smem);
-  if (e == cudaSuccess) e = opt_fwd.ensure(k_fwd, (int)G::row_smem);
+  if (e == cudaSuccess) e = opt_fwd.ensure(k_fwd, (int)FG::smem);
   if (e != cudaSuccess) return e;
   k_in<<<dim3(MR / G::RB, L.ntasks, nimg), NT, G::row_smem, stream>>>(L, F);
   k_cols<<<dim3(MC / G::CB, L.ntasks, nimg), NT, G::col_smem, stream>>>(L);
-  if (L.modulus) k_fwd<<<dim3(MR / G::RB, L.ntasks, nimg), NT, G::row_smem, stream>>>(L, F);
+  if (L.modulus) k_fwd<<<dim3(FG::blocks, L.ntasks, nimg), NT, FG::smem, stream>>>(L, F);
   if (!L.skip_s) k_lp<<<dim3(L.ntasks, nimg), NT, lp_smem, stream>>>(L, F);
   return cudaGetLastError();
 }

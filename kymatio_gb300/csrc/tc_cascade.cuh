@@ -78,33 +78,45 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
   }
   if (tid == 0) tc::mbar_init(mbar, 1);
 
-  // Operand B first: its loads from the low-pass table overlap the fold
-  // below (its region is disjoint from the FFT array).
+  // Operand B = T_c (NP x KP, rows beyond NOUTC and columns beyond MC zero):
+  // its values are loaded into registers here and split into the operand
+  // after the fold, so the loads' latency overlaps the fold's.
   constexpr int G8 = KP / 8;  // 16-byte chunks per operand row
-  // B = T_c (NP x KP, rows beyond NOUTC and columns beyond MC zero)
+  constexpr int BPER = (NP * G8 + NT - 1) / NT;
   const float* tcm = LP.c[t.phi];
   const size_t b_half = (size_t)NP * KP * 2;
-  for (int g = tid; g < NP * G8; g += NT) {
-    const int r = g % NP, c = g / NP;
-    uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
-    if (r < NOUTC) {
+  float bval[BPER][8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int k = 8 * c + q;
-        const float v = k < MC ? __ldg(tcm + r * MC + k) : 0.f;
-        __nv_bfloat16 bh, bl;
-        tc::split_bf16(v, bh, bl);
-        h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
-        l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
-      }
+  for (int i = 0; i < BPER; ++i) {
+    const int g = tid + i * NT;
+    const int r = g % NP, c = g / NP;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = 8 * c + q;
+      bval[i][q] = (g < NP * G8 && r < NOUTC && k < MC) ? __ldg(tcm + r * MC + k) : 0.f;
     }
-    const uint32_t off = tc::kmajor_offset(r, 8 * c, KP);
-    *reinterpret_cast<uint4*>(bop + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4*>(bop + b_half + off) = make_uint4(l[0], l[1], l[2], l[3]);
   }
 
   // ---- U = |IFFT2(fold(src * psi))| -----------------------------------------
   ct_load<MR, MC, 1, false, NT, KF, LD>(A, L, F, t, img, 0);
+#pragma unroll
+  for (int i = 0; i < BPER; ++i) {
+    const int g = tid + i * NT;
+    if (g < NP * G8) {
+      const int r = g % NP, c = g / NP;
+      uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        __nv_bfloat16 bh, bl;
+        tc::split_bf16(bval[i][q], bh, bl);
+        h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
+        l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
+      }
+      const uint32_t off = tc::kmajor_offset(r, 8 * c, KP);
+      *reinterpret_cast<uint4*>(bop + off) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4*>(bop + b_half + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
   __syncthreads();
   ct::fft_lines<MC, MR, NT>(ct::RowLines<LD, false>{A}, 0, L.prow.tw, true);
   ct::fft_lines<MR, MC, NT>(ct::ColLines<LD>{A}, 0, L.pcol.tw, true);
