@@ -26,7 +26,8 @@ namespace kym {
 
 constexpr int kLinesPerCta = 16;
 constexpr int kLinesThreads = 256;
-constexpr int kLinesMinBlocks = 3;  // CTAs per SM the register budget is sized for
+constexpr int kLinesMinBlocks = 3;  // CTAs per SM the register budget is sized for (80 registers)
+constexpr int kRowsFwdMinBlocks = 4;  // the row-FFT pass fits 64 registers (folds of at most 8 rows)
 
 // Copy n <= N complex elements from global to shared memory with every load
 // of a thread issued before its first store (N / NT loads in flight per
@@ -73,12 +74,24 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
   const int r0 = blockIdx.x * RB;
   constexpr int NEL = RB * MC;
   if (KF == 0 || (KF < 0 && L.src_image)) {
+    // reflect-padded image rows, every load of a thread in flight before the first store
     const float* x = L.x + (size_t)(L.img0 + img) * L.x_stride;
-    for (int e = threadIdx.x; e < NEL; e += NT) {
-      const int u = e / MC, v = e % MC;
-      const int iy = ct_reflect(r0 + u - L.pad_t, L.img_M);
-      const int ix = ct_reflect(v - L.pad_l, L.img_N);
-      A[u * LDR + v] = make_float2(__ldg(x + (size_t)iy * L.img_N + ix) * L.load_scale, 0.f);
+    constexpr int PER = (NEL + NT - 1) / NT;
+    float xv[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int e = threadIdx.x + i * NT;
+      if (e < NEL) {
+        const int u = e / MC, v = e % MC;
+        const int iy = ct_reflect(r0 + u - L.pad_t, L.img_M);
+        const int ix = ct_reflect(v - L.pad_l, L.img_N);
+        xv[i] = __ldg(x + (size_t)iy * L.img_N + ix);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int e = threadIdx.x + i * NT;
+      if (e < NEL) A[(e / MC) * LDR + e % MC] = make_float2(xv[i] * L.load_scale, 0.f);
     }
   } else if constexpr (KF > 0) {
     static_assert(MC % 2 == 0, "paired columns");
@@ -280,13 +293,14 @@ __device__ __forceinline__ void rows_fwd_map(int b, int i, int& grow, int& src, 
 }
 
 template <int MR, int MC, int SR, int SC, int NT>
-__global__ void __launch_bounds__(NT, kLinesMinBlocks)
+__global__ void __launch_bounds__(NT, MR / SR > 8 ? kLinesMinBlocks : kRowsFwdMinBlocks)
     lines_rows_fwd_kernel(const __grid_constant__ CascadeLaunch L, const __grid_constant__ FilterTable F) {
   using G = RowsFwdGeom<MR, MC, SR, SC>;
   constexpr int KSR = G::KSR, KSC = G::KSC, RB = G::RB, LDR = G::LDR;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* A = reinterpret_cast<float2*>(smem_raw);
   __shared__ int s_grow[RB], s_src[RB];
+  __shared__ unsigned char s_loc[MR];  // global row -> local row (the block's rows only)
   const int task = blockIdx.y;
   const Task t = L.tasks[task];
   const int img = blockIdx.z;
@@ -297,6 +311,7 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
     rows_fwd_map<MR, SR>(b, threadIdx.x, g, src, nc);
     s_grow[threadIdx.x] = g;
     s_src[threadIdx.x] = src;
+    s_loc[g] = (unsigned char)threadIdx.x;
   }
   __syncthreads();
   const int ncomp = b > 0 ? KSR : KSR + 1;
@@ -320,26 +335,42 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
   if (L.skip_s) return;
   const float* phi = F.f[t.phi];
   float2* bsum = L.dst + (size_t)img * L.dst_stride + L.bsum_off + (size_t)task * SR * SC;
-  // the block's two classes: c0 = b (or 0) and c1 = SR - b (or SR / 2); local
-  // rows of class c, a-th alias: found by global row in s_grow
-  for (int e = threadIdx.x; e < 2 * SC; e += NT) {
-    const int ci = e / SC, q = e % SC;
-    const int p = b > 0 ? (ci ? SR - b : b) : (ci ? SR / 2 : 0);
+  // The block's two classes c = cls[0], cls[1]: folded row c of B sums the
+  // KSR rows c + SR a.  Four threads per output element each take KSR / 4
+  // aliases (their loads unrolled and in flight together); a shuffle adds
+  // the four partial sums.
+  constexpr int SPL = 4, APT = KSR / SPL;
+  static_assert(KSR % SPL == 0 && NT % 32 == 0, "split of the fold");
+  const int cls[2] = {b > 0 ? b : 0, b > 0 ? SR - b : SR / 2};
+  constexpr int NITEM = 2 * SC * SPL;
+  for (int base = 0; base < NITEM; base += NT) {
+    const int e = base + threadIdx.x;
+    const int sub = e % SPL, o = e / SPL;
+    const int ci = o / SC, q = o % SC;
     float2 acc = make_float2(0.f, 0.f);
-    for (int i = 0; i < RB; ++i) {
-      const int g = s_grow[i];
-      if (g % SR != p) continue;
-      const float2* row = A + i * LDR;
-      const float* frow = phi + (size_t)g * MC;
+    if (e < NITEM) {
+      const int p = cls[ci];
 #pragma unroll
-      for (int bb = 0; bb < KSC; ++bb) {
-        const float2 z = row[q + SC * bb];
-        const float f = __ldg(frow + q + SC * bb);
-        acc.x = fmaf(z.x, f, acc.x);
-        acc.y = fmaf(z.y, f, acc.y);
+      for (int k = 0; k < APT; ++k) {
+        const int a = sub * APT + k;
+        const int g = p + SR * a;  // its local row: the one of s_grow equal to g
+        const float2* row = A + s_loc[g] * LDR;
+        const float* frow = phi + (size_t)g * MC;
+#pragma unroll
+        for (int bb = 0; bb < KSC; ++bb) {
+          const float2 z = row[q + SC * bb];
+          const float f = __ldg(frow + q + SC * bb);
+          acc.x = fmaf(z.x, f, acc.x);
+          acc.y = fmaf(z.y, f, acc.y);
+        }
       }
     }
-    bsum[p * SC + q] = cscale(acc, L.s_scale);
+#pragma unroll
+    for (int m = 1; m < SPL; m <<= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, m);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, m);
+    }
+    if (e < NITEM && sub == 0) bsum[cls[ci] * SC + q] = cscale(acc, L.s_scale);
   }
 }
 
