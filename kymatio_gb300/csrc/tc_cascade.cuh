@@ -104,14 +104,9 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
     const int g = tid + i * NT;
     if (g < NP * G8) {
       const int r = g % NP, c = g / NP;
-      uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
+      uint32_t h[4], l[4];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        __nv_bfloat16 bh, bl;
-        tc::split_bf16(bval[i][q], bh, bl);
-        h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
-        l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
-      }
+      for (int q = 0; q < 4; ++q) tc::split2_bf16(bval[i][2 * q], bval[i][2 * q + 1], h[q], l[q]);
       const uint32_t off = tc::kmajor_offset(r, 8 * c, KP);
       *reinterpret_cast<uint4*>(bop + off) = make_uint4(h[0], h[1], h[2], h[3]);
       *reinterpret_cast<uint4*>(bop + b_half + off) = make_uint4(l[0], l[1], l[2], l[3]);
@@ -139,19 +134,18 @@ __global__ void __launch_bounds__(NT, occupancy_blocks(TcGeom<MR, MC, NOUTC>::sm
       const int c = g / MR8;
       uint32_t h[4] = {0, 0, 0, 0}, l[4] = {0, 0, 0, 0};
       if (r < MR) {
+        float uv[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int k = 8 * c + q;
-          float uv = 0.f;
+          uv[q] = 0.f;
           if (k < MC) {
             const float2 z = A[r * LD + k];
-            uv = tc::sqrt_approx(fmaf(z.x, z.x, z.y * z.y));
+            uv[q] = tc::sqrt_approx(fmaf(z.x, z.x, z.y * z.y));
           }
-          __nv_bfloat16 bh, bl;
-          tc::split_bf16(uv, bh, bl);
-          h[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * (q & 1));
-          l[q >> 1] |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * (q & 1));
         }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tc::split2_bf16(uv[2 * q], uv[2 * q + 1], h[q], l[q]);
       }
       hi4[i] = make_uint4(h[0], h[1], h[2], h[3]);
       lo4[i] = make_uint4(l[0], l[1], l[2], l[3]);
