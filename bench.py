@@ -534,7 +534,38 @@ def _extra_jtfs_8192(dev, flush, steps, warmup):
     return {'sig_s': B / ms * 1e3, 'channels': int(S(xs[:1]).shape[-2]), 'cpu_baseline': cpu}
 
 
+def _extra_filter_bank(dev, flush, steps, warmup):
+    """Construction of the 2-D filter bank at 256x256 J=3 (padded 272, L=8)
+    and 256x256 J=4 (padded 288): the host build (bit for bit the
+    reference's), the device build (FP64 on the GPU), and the reference's
+    own constructor on the host cores."""
+    import torch
+    from kymatio_gb300.filter_bank import filter_bank_2d, filter_bank_2d_device
+    res = {}
+    for (Mp, J_) in ((272, 3), (288, 4)):
+        filter_bank_2d.cache_clear()
+        t = time.perf_counter()
+        filter_bank_2d(Mp, Mp, J_, 8)
+        host_s = time.perf_counter() - t
+        filter_bank_2d_device(Mp, Mp, J_, 8)  # first call: module load
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(3):
+            filter_bank_2d_device(Mp, Mp, J_, 8)
+        torch.cuda.synchronize()
+        dev_s = (time.perf_counter() - t) / 3
+        r = {'host_s': host_s, 'device_s': dev_s}
+        if CTX['cpu'] and reference_kymatio() is not None:
+            from kymatio.scattering2d.filter_bank import filter_bank as ref_bank
+            t = time.perf_counter()
+            ref_bank(Mp, Mp, J_, 8)
+            r['reference_host_s'] = time.perf_counter() - t
+        res['padded_%d_J%d' % (Mp, J_)] = r
+    return res
+
+
 EXTRAS = {
+    'filter_bank_construction': _extra_filter_bank,
     'scattering2d_32x32_J2_b128': _extra_s2d_32,
     'jtfs_8192_J6_Jfr2_Q8_2_b64': _extra_jtfs_8192,
     'scattering1d_8192_J6_Q8_T64_b256': _extra_s1d_8192,

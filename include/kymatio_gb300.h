@@ -118,6 +118,21 @@ int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores)
  * counterpart in the reference (profiling). */
 int kym_s2d_group_launches(const kym_s2d_plan* plan, int group, int batch, int tensor_cores);
 
+/* Device build of the 2-D filter bank (replaces the host construction of
+ * kymatio/scattering2d/filter_bank.py:5-175 called by ScatteringBase2D.
+ * create_filters, kymatio/scattering2d/frontend/base_frontend.py:34-36):
+ * the Gaussian low-pass phi and the J x L Morlet wavelets at the padded size,
+ * every level cropped by the masked alias sum, computed in FP64 on the device
+ * and rounded once to float32.  `out` receives
+ * kym_s2d_filter_bank_floats() floats: the levels of phi, then of every psi
+ * (j-major, theta-minor), each level row-major -- the order of the
+ * reference's tensor{n} buffers.  The values agree with the reference's
+ * complex64 build to float32 rounding, not bit for bit. */
+long long kym_s2d_filter_bank_floats(int M_padded, int N_padded, int J, int L);
+size_t kym_s2d_filter_bank_workspace_bytes(int M_padded, int N_padded, int J, int L);
+int kym_s2d_filter_bank(int M_padded, int N_padded, int J, int L, float* out, long long out_floats, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* Hand-written backward: grad_x (batch, M, N) = (d forward / d x)^T grad_out,
  * grad_out shaped like the forward's output.  Replaces torch autograd through
  * the reference op surface (unpad, irfft, subsample_fourier, cdgmm, rfft,

@@ -50,6 +50,9 @@ SIGNATURES = {
                                     ctypes.POINTER(ctypes.c_float), _c_int]),
     'kym_s2d_group_kernels': (_c_int, [_vp, _c_int, _c_int]),
     'kym_s2d_group_launches': (_c_int, [_vp, _c_int, _c_int, _c_int]),
+    'kym_s2d_filter_bank_floats': (ctypes.c_longlong, [_c_int] * 4),
+    'kym_s2d_filter_bank_workspace_bytes': (_c_size, [_c_int] * 4),
+    'kym_s2d_filter_bank': (_c_int, [_c_int] * 4 + [_vp, ctypes.c_longlong, _vp, _c_size, _vp]),
     'kym_s2d_group_uses_tc': (_c_int, [_vp, _c_int]),
     'kym_tc_selftest': (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _vp, _vp]),
     'kym_s2d_group_count': (_c_int, [_vp]),

@@ -13,7 +13,7 @@ import torch
 import torch.nn as nn
 
 from . import _autograd, _lib
-from .filter_bank import filter_bank_2d, padded_size_2d, separable_lowpass
+from .filter_bank import filter_bank_2d, filter_bank_2d_device, padded_size_2d, separable_lowpass
 
 
 class Scattering2D(nn.Module):
@@ -27,9 +27,14 @@ class Scattering2D(nn.Module):
     selects the tensor-core split-precision form: paths without children
     compute their low-pass branch as a separable product on tcgen05 (BF16
     hi/lo operands, FP32 accumulation); ``tensor_cores`` toggles it later.
+
+    filters='host' (default) builds the filter bank on the host, bit for bit
+    the reference's; filters='device' builds it on the current CUDA device
+    (FP64, rounded to float32: equal to float32 rounding) and registers the
+    buffers there, which takes milliseconds instead of seconds at large sizes.
     """
 
-    def __init__(self, J, shape, L=8, max_order=2, pre_pad=False, backend='torch', out_type='array'):
+    def __init__(self, J, shape, L=8, max_order=2, pre_pad=False, backend='torch', out_type='array', filters='host'):
         super().__init__()
         self.frontend_name = 'torch'
         if backend is not None and not isinstance(backend, str) and \
@@ -46,16 +51,23 @@ class Scattering2D(nn.Module):
         self._M_padded, self._N_padded = padded_size_2d(M, N, self.J)
         self.pad_size = [(self._M_padded - M) // 2, (self._M_padded - M + 1) // 2,
                          (self._N_padded - N) // 2, (self._N_padded - N + 1) // 2]
-        phi, psi = filter_bank_2d(self._M_padded, self._N_padded, self.J, self.L)
+        if filters == 'device':
+            phi, psi = filter_bank_2d_device(self._M_padded, self._N_padded, self.J, self.L)
+            as_buffer = lambda lv: lv.clone().unsqueeze(-1)  # noqa: E731
+        elif filters == 'host':
+            phi, psi = filter_bank_2d(self._M_padded, self._N_padded, self.J, self.L)
+            as_buffer = lambda lv: torch.from_numpy(lv.copy()).unsqueeze(-1)  # noqa: E731
+        else:
+            raise ValueError("filters must be 'host' or 'device'")
         self.phi = {'levels': list(phi), 'j': self.J}
         self.psi = [{'levels': list(p['levels']), 'j': p['j'], 'theta': p['theta']} for p in psi]
         n = 0
         for lv in self.phi['levels']:
-            self.register_buffer('tensor' + str(n), torch.from_numpy(lv.copy()).unsqueeze(-1))
+            self.register_buffer('tensor' + str(n), as_buffer(lv))
             n += 1
         for p in self.psi:
             for lv in p['levels']:
-                self.register_buffer('tensor' + str(n), torch.from_numpy(lv.copy()).unsqueeze(-1))
+                self.register_buffer('tensor' + str(n), as_buffer(lv))
                 n += 1
         self._n_filters = n
         self._plan = None
@@ -66,10 +78,15 @@ class Scattering2D(nn.Module):
         # separable factors of every low-pass level (non-persistent: derived from tensor{j})
         s_r, s_c = self._M_padded // 2 ** self.J, self._N_padded // 2 ** self.J
         for j, lv in enumerate(self.phi['levels']):
-            Tr, Tc, _ = separable_lowpass(lv, 1, s_r - 2, 1, s_c - 2, 2 ** (self.J - j), 2 ** (self.J - j))
-            self.register_buffer('lowpass_r' + str(j), torch.from_numpy(Tr.astype('float32')), persistent=False)
-            self.register_buffer('lowpass_c' + str(j), torch.from_numpy(Tc.astype('float32')), persistent=False)
-        self.register_buffer('_tc_status', torch.zeros(1, dtype=torch.int32), persistent=False)
+            dev = lv.device if torch.is_tensor(lv) else torch.device('cpu')
+            lvh = lv.cpu().numpy() if torch.is_tensor(lv) else lv
+            Tr, Tc, _ = separable_lowpass(lvh, 1, s_r - 2, 1, s_c - 2, 2 ** (self.J - j), 2 ** (self.J - j))
+            self.register_buffer('lowpass_r' + str(j), torch.from_numpy(Tr.astype('float32')).to(dev),
+                                 persistent=False)
+            self.register_buffer('lowpass_c' + str(j), torch.from_numpy(Tc.astype('float32')).to(dev),
+                                 persistent=False)
+        self.register_buffer('_tc_status', torch.zeros(1, dtype=torch.int32, device=self.tensor0.device),
+                             persistent=False)
 
     # -- plan ---------------------------------------------------------------
     def _get_plan(self):
