@@ -89,6 +89,48 @@ __global__ void __launch_bounds__(kThreads, 1) op_fft2_kernel(const __grid_const
   }
 }
 
+// Many short 1-D lines per CTA: lines are the local rows of an odd-pitch
+// array (pitch L.ld), transformed by the row pass of the 2-D engine.  The
+// one-CTA-per-line kernel above leaves most of a CTA idle on lines of a
+// few dozen points (the frequency axis of joint time-frequency scattering
+// transforms tens of thousands of them per call).
+__global__ void __launch_bounds__(kThreads) op_fft_lines_kernel(const __grid_constant__ OpFftLaunch L,
+                                                                long long nlines, int lpc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* A = reinterpret_cast<float2*>(smem_raw);
+  const long long l0 = (long long)blockIdx.x * lpc;
+  const int nl = (int)min((long long)lpc, nlines - l0);
+  const int N = L.N, ld = L.ld;
+  const size_t base = (size_t)l0 * N;
+  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
+    float2 v;
+    if (L.in_real) v = make_float2(__ldg(L.in + base + e), 0.f);
+    else v = __ldg(reinterpret_cast<const float2*>(L.in) + base + e);
+    A[(e / N) * ld + e % N] = v;
+  }
+  __syncthreads();
+  Slab w;
+  w.local = A;
+  w.rowp = nullptr;
+  w.rows = nl;
+  w.cols = N;
+  w.ld = ld;
+  w.rows_local = nl;
+  w.row0 = 0;
+  w.nct = 1;
+  w.rank = 0;
+  fft_pass<true, false, false>(w, nl, 0, L.prow, L.inverse != 0, Barrier{false});
+  for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
+    const float2 v = A[(e / N) * ld + e % N];
+    if (L.out_real) L.out[base + e] = v.x * L.scale;
+    else reinterpret_cast<float2*>(L.out)[base + e] = make_float2(v.x * L.scale, v.y * L.scale);
+  }
+}
+
+// 1-D lines of at most this many points go through op_fft_lines_kernel
+constexpr int kShortLine = 2048;
+constexpr size_t kLinesSmem = 48 * 1024;  // shared memory per CTA of the short-line kernel
+
 namespace {
 
 struct OpPlan {
@@ -333,6 +375,21 @@ extern "C" int kym_op_fft2(const float* in, float* out, int batch, int M, int N,
   L.oned = P->oned;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e;
+  if (P->oned && N <= kShortLine) {
+    // many lines per CTA, odd pitch
+    OpFftLaunch Ls = L;
+    Ls.ld = (N % 2 == 0) ? N + 1 : N;
+    const int lpc = (int)std::max<size_t>(1, kLinesSmem / ((size_t)Ls.ld * sizeof(float2)));
+    const long long nblk = ((long long)batch + lpc - 1) / lpc;
+    const size_t smem = (size_t)std::min<long long>(lpc, batch) * Ls.ld * sizeof(float2);
+    op_fft_lines_kernel<<<(unsigned)nblk, kThreads, smem, s>>>(Ls, (long long)batch, lpc);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error_message("fft", cudaGetErrorString(e));
+      return KYM_ERR_CUDA;
+    }
+    return KYM_OK;
+  }
   for (int b0 = 0; b0 < batch; b0 += 1 << 20) {
     OpFftLaunch Lb = L;
     const size_t off = (size_t)b0 * M * N * (in_real ? 1 : 2);

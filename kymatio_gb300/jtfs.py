@@ -185,9 +185,13 @@ class TimeFrequencyScattering(Scattering1D):
     """Joint time-frequency scattering (kymatio.torch.TimeFrequencyScattering)."""
 
     def __init__(self, J, J_fr, Q, shape, T=None, stride=None, Q_fr=1, F=None, stride_fr=None, out_type='array',
-                 format='time', backend='torch'):
+                 format='time', backend='torch', graph=False):
         super().__init__(J, shape, Q=Q, T=T, stride=stride, max_order=2, oversampling=None, out_type=out_type,
                          backend=backend)
+        # graph=True: an array-output forward without autograd replays one CUDA
+        # graph per input shape (its thousands of small launches become one)
+        self.graph = graph
+        self._graphs = {}
         self.J_fr = J_fr
         self._F = F
         self.oversampling_fr = 0
@@ -290,7 +294,36 @@ class TimeFrequencyScattering(Scattering1D):
             raise TypeError('The input must be a CUDA tensor: the GB300 scattering engine runs on CUDA only.')
         if x.dtype != torch.float32:
             raise TypeError('The input must be float32 (got %s).' % x.dtype)
+        if self.graph and self.out_type == 'array' and not (torch.is_grad_enabled() and x.requires_grad):
+            return self._jtfs_graphed(x, backend1d)
         return self._jtfs(x, backend1d)
+
+    def _jtfs_graphed(self, x, B):
+        """The same forward replayed from a CUDA graph captured on first use
+        for this input shape and format (after an eager warm-up that creates
+        every plan and device table); the result is copied out of the graph's
+        buffers, so it stays valid across calls."""
+        key = (tuple(x.shape), str(x.device), self.format)
+        ent = self._graphs.get(key)
+        if ent is None:
+            static_x = x.detach().contiguous().clone()
+            with torch.no_grad():
+                self._jtfs(static_x, B)
+                torch.cuda.synchronize(x.device)
+                g = torch.cuda.CUDAGraph()
+                cap = torch.cuda.Stream(x.device)
+                cap.wait_stream(torch.cuda.current_stream(x.device))
+                with torch.cuda.graph(g, stream=cap):
+                    static_out = self._jtfs(static_x, B)
+            ent = self._graphs[key] = (g, static_x, static_out)
+        g, static_x, static_out = ent
+        static_x.copy_(x)
+        g.replay()
+        return static_out.clone()
+
+    def _apply(self, fn, *args, **kwargs):
+        self._graphs = {}  # the captured graphs hold the old buffers' addresses
+        return super()._apply(fn, *args, **kwargs)
 
     def _jtfs(self, x, B):
         """The transform over the op surface B (the CUDA ops in the module)."""

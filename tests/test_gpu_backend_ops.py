@@ -123,6 +123,25 @@ def test_fft_kat_and_round_trips(dev):
     assert 'must be contiguous' in e.value.args[0]
 
 
+@pytest.mark.parametrize('n,batch', [(64, 3000), (17, 700), (100, 51), (2048, 9), (4096, 5), (16384, 3)])
+def test_fft_1d_batches(dev, n, batch):
+    """Batches of 1-D lines through kym_op_fft2 (M = 1): short lines many per
+    CTA, long lines one per CTA; forward complex, inverse to real."""
+    from kymatio_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(n + batch)
+    a = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    at = torch.from_numpy(np.stack([a.real, a.imag], -1)).to(dev)
+    out = torch.empty_like(at)
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.check(lib.kym_op_fft2(at.data_ptr(), out.data_ptr(), batch, 1, n, 0, 0, 0, 1.0, st), 'fft')
+    got = out[..., 0].cpu().numpy() + 1j * out[..., 1].cpu().numpy()
+    assert rel_l2(got, np.fft.fft(a.astype(np.complex128), axis=-1)) < 1e-6
+    real = torch.empty((batch, n), device=dev)
+    _lib.check(lib.kym_op_fft2(out.data_ptr(), real.data_ptr(), batch, 1, n, 0, 1, 1, 1.0 / n, st), 'ifft')
+    assert rel_l2(real.cpu().numpy(), a.real) < 1e-6
+
+
 def test_stack(dev):
     from kymatio_gb300.backend import backend2d as B
     x, y, z = (torch.randn(3, 6, 6, device=dev) for _ in range(3))

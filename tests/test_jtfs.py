@@ -170,6 +170,31 @@ def test_jtfs_on_gpu(case):
     _check(case['name'], S(x), 1e-5)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize('case', [c for c in CASES if c['kwargs'].get('out_type', 'array') == 'array'],
+                         ids=lambda c: c['name'])
+def test_jtfs_graph_replay(case):
+    """graph=True replays a CUDA graph of the whole forward: the reference's
+    outputs on the golden input, then the eager forward on new data, twice."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from kymatio_gb300.jtfs import TimeFrequencyScattering
+    dev = torch.device('cuda:0')
+    S = TimeFrequencyScattering(**_kwargs(case), graph=True).to(dev)
+    x = torch.from_numpy(_D[case['name'] + '/x']).to(dev)
+    out = S(x)
+    assert len(S._graphs) == 1
+    _check(case['name'], out, 1e-5)
+    for _ in range(2):
+        x2 = torch.rand_like(x)
+        got = S(x2)
+        S.graph = False
+        ref = S(x2)
+        S.graph = True
+        assert torch.equal(got, ref)
+    assert torch.equal(out, S(x))  # earlier results are copies, not the graph's buffers
+
+
 GRAD_CASES = [c for c in CASES if c['name'] + '/gx' in _D.files]
 
 
