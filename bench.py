@@ -485,6 +485,20 @@ def _extra_mixed_512(dev, flush, steps, warmup):
     gr = _time_ms(lambda: mix.forward_grouped(xs), steps, warmup, flush)
     mixt = MixedScattering2D(list(xs), tensor_cores=True).to(dev)
     grt = _time_ms(lambda: mixt.forward_grouped(xs), steps, warmup, flush)
+    # autotuned: chunk and, in the tensor-core form, the kernel form per size
+    # (tuning cache in a temporary directory, so the run starts cold)
+    import tempfile
+    old_cache = os.environ.get('KYMATIO_GB300_CACHE')
+    with tempfile.TemporaryDirectory() as tmp:
+        os.environ['KYMATIO_GB300_CACHE'] = tmp
+        mixa = MixedScattering2D(list(xs), tensor_cores=True, tune=True).to(dev)
+        mixa.forward_grouped(xs)
+        tuned = {s: bool(m.tensor_cores) for s, m in ((int(k), v) for k, v in mixa.mods.items())}
+        gra = _time_ms(lambda: mixa.forward_grouped(xs), steps, warmup, flush)
+    if old_cache is None:
+        os.environ.pop('KYMATIO_GB300_CACHE', None)
+    else:
+        os.environ['KYMATIO_GB300_CACHE'] = old_cache
     cpu = None
     if CTX['cpu'] and reference_kymatio() is not None:
         # one reference module per side (its frontend fixes the shape), on a
@@ -500,8 +514,9 @@ def _extra_mixed_512(dev, flush, steps, warmup):
         cpu = {'value': 512 / tot, 'unit': 'img/s', 'cores': threads, 'kind': 'reference',
                'sample': '4 images per side, one stock ScatteringTorch2D per side, time scaled to the counts'}
     return {'img_s_per_size_sequential': 512 / seq * 1e3, 'img_s_graph': 512 / gr * 1e3,
-            'img_s_graph_tc': 512 / grt * 1e3, 'counts': {str(s): len(v) for s, v in sorted(groups.items())},
-            'cpu_baseline': cpu}
+            'img_s_graph_tc': 512 / grt * 1e3, 'img_s_graph_tc_autotuned': 512 / gra * 1e3,
+            'autotuned_tensor_cores': {str(k): v for k, v in sorted(tuned.items())},
+            'counts': {str(s): len(v) for s, v in sorted(groups.items())}, 'cpu_baseline': cpu}
 
 
 def _extra_jtfs_8192(dev, flush, steps, warmup):

@@ -6,8 +6,11 @@ group's fused cascade on its own CUDA stream.  The whole batch is captured
 once into a single CUDA graph (fork/join over the streams); later batches
 with the same composition replay it with one host launch, the size groups
 running concurrently on the GPU.  An autotuner (``autotune``) picks each
-size's parent-spectrum chunk (images per order-2 pass) by timing candidates,
-and caches the choice per (N, J, L, form, batch bucket) in a JSON file.
+size's parent-spectrum chunk (images per order-2 pass) and, when the
+tensor-core form is asked for, whether that size's kernels run in it or in the
+plain FP32 form (the more precise of the two, so either meets the tensor-core
+form's bar), by timing candidates; the choice is cached per (N, J, L, form,
+batch bucket) in a JSON file.
 """
 import json
 import math
@@ -48,8 +51,9 @@ def _store_cache(entries):
 
 def autotune(module, batch, steps=3, candidates=None):
     """Time chunk sizes (images per order-2 pass) for ``module`` at ``batch``
-    images and keep the fastest; cached per (N, J, L, form, batch bucket).
-    Returns the chosen chunk."""
+    images -- and, for a module in the tensor-core form, both kernel forms --
+    and keep the fastest; cached per (N, J, L, form, batch bucket).  Returns
+    the chosen chunk (the chosen form is left in ``module.tensor_cores``)."""
     from . import _lib
     form = 'tc' if module.tensor_cores else 'plain'
     bucket = 1 << max(0, math.ceil(math.log2(max(1, batch))))
@@ -58,6 +62,7 @@ def autotune(module, batch, steps=3, candidates=None):
         entries = _load_cache()
     if key in entries:
         module.set_chunk(entries[key]['chunk'])
+        module.tensor_cores = entries[key].get('tensor_cores', module.tensor_cores)
         return entries[key]['chunk']
     dev = module.tensor0.device
     plan = module._get_plan()
@@ -66,24 +71,29 @@ def autotune(module, batch, steps=3, candidates=None):
     if candidates is None:
         candidates = sorted({max(1, c) for c in (default // 4, default // 2, default, default * 2, batch)})
     x = torch.rand((batch,) + module.shape, device=dev)
+    forms = (True, False) if module.tensor_cores else (False,)
     best = None
-    for c in candidates:
-        module.set_chunk(c)
-        module(x)
-        torch.cuda.synchronize(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(steps):
-            module(x)
-        e1.record()
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        if best is None or ms < best[1]:
-            best = (c, ms)
+    with torch.no_grad():
+        for tc in forms:
+            module.tensor_cores = tc
+            for c in candidates:
+                module.set_chunk(c)
+                module(x)
+                torch.cuda.synchronize(dev)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(steps):
+                    module(x)
+                e1.record()
+                e1.synchronize()
+                ms = e0.elapsed_time(e1) / steps
+                if best is None or ms < best[1]:
+                    best = (c, ms, tc)
     module.set_chunk(best[0])
+    module.tensor_cores = best[2]
     with _CACHE_LOCK:
         entries = _load_cache()
-        entries[key] = {'chunk': best[0], 'ms': best[1]}
+        entries[key] = {'chunk': best[0], 'ms': best[1], 'tensor_cores': best[2]}
         _store_cache(entries)
     return best[0]
 
@@ -113,6 +123,7 @@ class MixedScattering2D(torch.nn.Module):
         self.graph = graph
         self.tune = tune
         self._graphs = {}
+        self._tuned = set()
 
     def _groups(self, images):
         idx = {}
@@ -139,9 +150,10 @@ class MixedScattering2D(torch.nn.Module):
         By default they are copied out first."""
         key = tuple(sorted((s, tuple(x.shape)) for s, x in xs.items()))
         dev = next(iter(xs.values())).device
-        if self.tune:
+        if self.tune and key not in self._tuned:  # once per composition
             for s, x in xs.items():
                 autotune(self.mods[str(s)], x.shape[0])
+            self._tuned.add(key)
         if not self.graph:
             streams = [torch.cuda.Stream(dev) for _ in xs]
             return self._run_groups(xs, streams)  # fresh outputs every call

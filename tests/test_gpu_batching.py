@@ -63,3 +63,25 @@ def test_mixed_batch_outputs_not_aliased():
     torch.cuda.synchronize()
     for s in xs:
         assert torch.equal(first[s], keep[s])
+
+
+def test_autotune_picks_a_form_per_size(tmp_path, monkeypatch):
+    """In the tensor-core form the autotuner may keep a size in the plain
+    form (more precise); either way the results meet the tensor-core bar and
+    the choice is cached."""
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    monkeypatch.setenv('KYMATIO_GB300_CACHE', str(tmp_path))
+    import json
+    from kymatio_gb300.batching import MixedScattering2D, default_J
+    from oracle.scattering2d import Scattering2D as Oracle
+    dev = torch.device('cuda:0')
+    rng = np.random.default_rng(6)
+    xs = {s: torch.from_numpy(rng.random((3, s, s)).astype(np.float32)).to(dev) for s in (32, 128)}
+    M = MixedScattering2D(list(xs), tensor_cores=True, tune=True).to(dev)
+    out = M.forward_grouped(xs)
+    entries = json.load(open(tmp_path / 'autotune.json'))
+    assert all('tensor_cores' in v for v in entries.values()) and len(entries) == 2
+    for s, x in xs.items():
+        ref = Oracle(default_J(s), (s, s))(x.cpu().numpy().astype(np.float64))
+        assert rel_l2(out[s].cpu().numpy(), ref) <= 5e-5
