@@ -172,6 +172,31 @@ struct RtEngine {
   }
 };
 
+// Loop over n elements, NT threads, with the loads of UNR iterations of a
+// thread issued before any of their uses (load(i) -> value, use(i, value)).
+template <int UNR, int NT, class LoadF, class UseF>
+__device__ __forceinline__ void staged_for(int n, LoadF load, UseF use) {
+  using T = decltype(load(0));
+  for (int base = 0; base < n; base += NT * UNR) {
+    T v[UNR];
+#pragma unroll
+    for (int k = 0; k < UNR; ++k) {
+      const int i = base + threadIdx.x + k * NT;
+      if (i < n) v[k] = load(i);
+    }
+#pragma unroll
+    for (int k = 0; k < UNR; ++k) {
+      const int i = base + threadIdx.x + k * NT;
+      if (i < n) use(i, v[k]);
+    }
+  }
+}
+
+struct PhiPre {
+  float f;
+  float2 y;
+};
+
 // ---------------------------------------------------------------------------
 // The backward task kernel body.
 // ---------------------------------------------------------------------------
@@ -210,24 +235,32 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
   // 2. g_U^ = phi * tile(g_B) / ks^2 + sum_c psi_c * tile(g_Y_c) / k_c^2
   const float* phi = F.f[t.phi];
   const int nloc = RL * MC;
-  for (int i = threadIdx.x; i < nloc; i += NT) {
-    const int u = i / MC, v = i % MC;
-    const int gu = row0 + u;
-    const float f = __ldg(phi + (size_t)gu * MC + v) * L.gb_scale;
-    const float2 b = *bat(gu % SR, v % SC);
-    *at(u, v) = make_float2(b.x * f, b.y * f);
-  }
   // children's contributions, summed beforehand by bwd_gather_kernel into
-  // this task's gradient block (complex, full m x m)
-  if (t.gather_count > 0) {
-    const float2* pre = L.gy + (size_t)img * L.gy_stride + t.gy_off + (size_t)row0 * MC;
-    for (int i = threadIdx.x; i < nloc; i += NT) {
-      const float2 y = __ldg(pre + i);
-      float2* p = at(i / MC, i % MC);
-      p->x += y.x;
-      p->y += y.y;
-    }
-  }
+  // this task's gradient block (complex, full m x m), added after the
+  // low-pass term (same order as before: phi term, then the children's sum)
+  const float2* pre =
+      t.gather_count > 0 ? L.gy + (size_t)img * L.gy_stride + t.gy_off + (size_t)row0 * MC : nullptr;
+  staged_for<8, NT>(
+      nloc,
+      [&](int i) {
+        const int u = i / MC, v = i % MC;
+        PhiPre r;
+        r.f = __ldg(phi + (size_t)(row0 + u) * MC + v);
+        r.y = pre ? __ldg(pre + i) : make_float2(0.f, 0.f);
+        return r;
+      },
+      [&](int i, const PhiPre& r) {
+        const int u = i / MC, v = i % MC;
+        const int gu = row0 + u;
+        const float f = r.f * L.gb_scale;
+        const float2 b = *bat(gu % SR, v % SC);
+        float2 z = make_float2(b.x * f, b.y * f);
+        if (pre) {
+          z.x += r.y.x;
+          z.y += r.y.y;
+        }
+        *at(u, v) = z;
+      });
   __syncthreads();
 
   // 3. g_U = Re IFFT2u(g_U^)
@@ -251,11 +284,14 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
   __syncthreads();  // g_U stores visible to this CTA before they are re-read in step 5
   if (L.ysaved) {
     const float2* ys = L.ysaved + (size_t)img * L.ysaved_stride + t.y_off;
-    for (int i = threadIdx.x; i < nloc; i += NT) {
-      const int u = i / MC, v = i % MC;
-      const int grow = E::kPerm ? e.rank + L.cluster * u : row0 + u;
-      *at(u, v) = __ldg(ys + (size_t)grow * MC + v);
-    }
+    staged_for<8, NT>(
+        nloc,
+        [&](int i) {
+          const int u = i / MC, v = i % MC;
+          const int grow = E::kPerm ? e.rank + L.cluster * u : row0 + u;
+          return __ldg(ys + (size_t)grow * MC + v);
+        },
+        [&](int i, const float2& y) { *at(i / MC, i % MC) = y; });
     __syncthreads();
   } else {
     const float2* src = L.src + (size_t)img * L.src_stride + t.src_off;
@@ -281,13 +317,14 @@ __device__ __forceinline__ void bwd_body(const E& e, const BwdLaunch& L, const F
   }
 
   // 5. g_y = g_U * y / |y|  (zero where |y| == 0)
-  for (int i = threadIdx.x; i < nloc; i += NT) {
-    float2* p = at(i / MC, i % MC);
-    const float2 y = *p;
-    const float m = sqrtf(fmaf(y.x, y.x, y.y * y.y));
-    const float g = gu_out[i];
-    *p = (m > 0.f) ? make_float2(g * y.x / m, g * y.y / m) : make_float2(0.f, 0.f);
-  }
+  staged_for<8, NT>(
+      nloc, [&](int i) { return gu_out[i]; },
+      [&](int i, const float& g) {
+        float2* p = at(i / MC, i % MC);
+        const float2 y = *p;
+        const float m = sqrtf(fmaf(y.x, y.x, y.y * y.y));
+        *p = (m > 0.f) ? make_float2(g * y.x / m, g * y.y / m) : make_float2(0.f, 0.f);
+      });
   __syncthreads();
 
   // 6. g_Y = FFT2(g_y) / m^2, written over g_U (already consumed)
