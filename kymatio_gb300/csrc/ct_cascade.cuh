@@ -231,15 +231,84 @@ __global__ void __launch_bounds__(NT, (CtGeom<MR, MC, SR, SC, C, ONED, NT>::kMin
     if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, true, true);
     // y saved for the backward in natural rows (a cluster holds row rank + C u)
     float2* ys = (L.ysave && t.y_off >= 0) ? L.ysave + (size_t)img * L.ysave_stride + t.y_off : nullptr;
-    for (int e = threadIdx.x; e < NLOC; e += NT) {
-      float2* p = at(e / MC, e % MC);
-      const float2 z = *p;
-      if (ys) ys[(size_t)(C > 1 ? rank + C * (e / MC) : e / MC) * MC + e % MC] = z;
-      *p = make_float2(sqrtf(fmaf(z.x, z.x, z.y * z.y)), 0.f);
+    if constexpr (C == 1 && !ONED && MR % 2 == 0 && MC % 2 == 0) {
+      // FFT2 of the real U: the column FFT runs two columns per complex line,
+      // Z = U[:, 2j] + i U[:, 2j+1] in column j; the unpacked columns
+      // X_2j[k] = (Z_k + conj Z_-k) / 2, X_2j+1[k] = -i (Z_k - conj Z_-k) / 2
+      // are Hermitian in k to the bit, so the row FFTs of rows 0 .. MR/2 give
+      // the rest as F[MR - k][v] = conj F[k][(MC - v) % MC].  In-place
+      // rewrites read into registers, then write after a barrier.
+      constexpr int HC = MC / 2, HR = MR / 2;
+      constexpr int NPAIR = MR * HC, PP = (NPAIR + NT - 1) / NT;
+      float2 m[PP];
+#pragma unroll
+      for (int i = 0; i < PP; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < NPAIR) {
+          const int r = e / HC, j = e % HC;
+          const float2 z0 = A[r * LD + 2 * j], z1 = A[r * LD + 2 * j + 1];
+          if (ys) {  // saved for the backward
+            ys[(size_t)r * MC + 2 * j] = z0;
+            ys[(size_t)r * MC + 2 * j + 1] = z1;
+          }
+          m[i] = make_float2(sqrtf(fmaf(z0.x, z0.x, z0.y * z0.y)), sqrtf(fmaf(z1.x, z1.x, z1.y * z1.y)));
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < PP; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < NPAIR) A[(e / HC) * LD + e % HC] = m[i];
+      }
+      __syncthreads();
+      ct::fft_lines<MR, HC, NT>(ct::ColLines<LD>{A}, 0, L.pcol.tw, false);
+      constexpr int NU = (HR + 1) * HC, PU = (NU + NT - 1) / NT;
+      float2 za[PU], zb[PU];
+#pragma unroll
+      for (int i = 0; i < PU; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < NU) {
+          const int k = e / HC, j = e % HC;
+          za[i] = A[k * LD + j];
+          zb[i] = A[((MR - k) % MR) * LD + j];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < PU; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < NU) {
+          const int k = e / HC, j = e % HC, km = (MR - k) % MR;
+          const float2 a = za[i], b = zb[i];
+          const float2 x0 = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+          const float2 x1 = make_float2(0.5f * (a.y + b.y), 0.5f * (b.x - a.x));
+          A[k * LD + 2 * j] = x0;
+          A[k * LD + 2 * j + 1] = x1;
+          if (km != k) {
+            A[km * LD + 2 * j] = make_float2(x0.x, -x0.y);
+            A[km * LD + 2 * j + 1] = make_float2(x1.x, -x1.y);
+          }
+        }
+      }
+      __syncthreads();
+      ct::fft_lines<MC, HR + 1, NT>(rows, 0, L.prow.tw, false);
+      for (int e = threadIdx.x; e < (MR - HR - 1) * MC; e += NT) {
+        const int r = HR + 1 + e / MC, v = e % MC;
+        const float2 z = A[(MR - r) * LD + (MC - v) % MC];
+        A[r * LD + v] = make_float2(z.x, -z.y);
+      }
+      __syncthreads();
+    } else {
+      for (int e = threadIdx.x; e < NLOC; e += NT) {
+        float2* p = at(e / MC, e % MC);
+        const float2 z = *p;
+        if (ys) ys[(size_t)(C > 1 ? rank + C * (e / MC) : e / MC) * MC + e % MC] = z;
+        *p = make_float2(sqrtf(fmaf(z.x, z.x, z.y * z.y)), 0.f);
+      }
+      __syncthreads();
+      if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, false, false);
+      ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, false);
     }
-    __syncthreads();
-    if constexpr (!ONED) ct_cols<MR, MC, C, LD, NT>(A, rank, L.pcol.tw, L.tw_rl, false, false);
-    ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, false);
   } else {
     // the input stage: natural rows for one CTA, permuted rows for a cluster
     ct::fft_lines<MC, RL, NT>(rows, 0, L.prow.tw, false);
