@@ -848,6 +848,10 @@ def main():
     ap.add_argument('--batch', type=int, default=64, help='images per GPU (64 is the benchmark workload)')
     ap.add_argument('--extra', choices=sorted(EXTRAS), default=None,
                     help='run only this other workload (for profiling) and print its JSON line')
+    ap.add_argument('--forwards', default=None,
+                    help='comma-separated forms (plain, tc): run --repeat forwards of each on the benchmark batch '
+                         '(--batch images) and exit; for ncu launch lists and captures')
+    ap.add_argument('--repeat', type=int, default=3)
     args = ap.parse_args()
     global BATCH
     BATCH = args.batch
@@ -855,6 +859,17 @@ def main():
     if args.impl == 'reference':
         world, rank = int(os.environ.get('WORLD_SIZE', '1')), int(os.environ.get('RANK', '0'))
         run_reference(args, world, rank)
+        return
+    if args.forwards:
+        import torch
+        from kymatio_gb300 import Scattering2D
+        dev = torch.device('cuda', 0)
+        x = torch.from_numpy(grf_batch(BATCH, seed=2)).to(dev)
+        for form in args.forwards.split(','):
+            S = Scattering2D(J, (SIDE, SIDE), L=L, backend={'plain': 'torch', 'tc': 'torch_tc'}[form]).to(dev)
+            for _ in range(args.repeat):
+                S(x)
+        torch.cuda.synchronize()
         return
     if args.extra:
         import torch
