@@ -466,6 +466,11 @@ def _extra_fwd_bwd_128(dev, flush, steps, warmup):
             'fwd_bwd_ms_recompute': fwdbwd_rc, 'ratio_recompute': fwdbwd_rc / fwd, 'cpu_baseline': cpu}
 
 
+def _lib_handle():
+    from kymatio_gb300 import _lib
+    return _lib.load()
+
+
 def _extra_mixed_512(dev, flush, steps, warmup):
     """512 images, sides drawn from {32,64,128,256}, seed 4: per-size launches
     vs one CUDA graph over grouped streams (plain and tensor-core forms)."""
@@ -493,7 +498,10 @@ def _extra_mixed_512(dev, flush, steps, warmup):
         os.environ['KYMATIO_GB300_CACHE'] = tmp
         mixa = MixedScattering2D(list(xs), tensor_cores=True, tune=True).to(dev)
         mixa.forward_grouped(xs)
-        tuned = {s: bool(m.tensor_cores) for s, m in ((int(k), v) for k, v in mixa.mods.items())}
+        lib = _lib_handle()
+        tuned = {int(k): sum(lib.kym_s2d_group_uses_tc(m._get_plan().h, g) > 0
+                             for g in range(lib.kym_s2d_group_count(m._get_plan().h)))
+                 for k, m in mixa.mods.items()}
         gra = _time_ms(lambda: mixa.forward_grouped(xs), steps, warmup, flush)
     if old_cache is None:
         os.environ.pop('KYMATIO_GB300_CACHE', None)
@@ -515,7 +523,7 @@ def _extra_mixed_512(dev, flush, steps, warmup):
                'sample': '4 images per side, one stock ScatteringTorch2D per side, time scaled to the counts'}
     return {'img_s_per_size_sequential': 512 / seq * 1e3, 'img_s_graph': 512 / gr * 1e3,
             'img_s_graph_tc': 512 / grt * 1e3, 'img_s_graph_tc_autotuned': 512 / gra * 1e3,
-            'autotuned_tensor_cores': {str(k): v for k, v in sorted(tuned.items())},
+            'autotuned_tensor_core_groups': {str(k): v for k, v in sorted(tuned.items())},
             'counts': {str(s): len(v) for s, v in sorted(groups.items())}, 'cpu_baseline': cpu}
 
 

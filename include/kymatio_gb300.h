@@ -107,6 +107,12 @@ int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int
 /* Tensor-core form of launch group `group` in kym_s2d_forward_tc: 0 none
  * (FP32 kernel), 1 the low-pass product on tcgen05, 2 the DFT-GEMM form. */
 int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);
+/* Let kym_s2d_forward_tc run group `group` in its tensor-core kernel
+ * (enable=1, the default) or in the plain FP32 kernel (enable=0; the plain
+ * form is the more precise, so the result stays within the tensor-core form's
+ * bar).  Used by the autotuner, which times both per group.  Returns the
+ * previous setting, or -1 for a bad group.  No counterpart in the reference. */
+int kym_s2d_set_group_tc(kym_s2d_plan* plan, int group, int enable);
 /* Kernels that group `group` launches per chunk of images: 1 for a fused
  * cascade kernel; 3 or 4 for the line-split passes of the sizes above one
  * CTA, per sub-launch (a sub-launch covers as many images as keep the

@@ -7,10 +7,10 @@ once into a single CUDA graph (fork/join over the streams); later batches
 with the same composition replay it with one host launch, the size groups
 running concurrently on the GPU.  An autotuner (``autotune``) picks each
 size's parent-spectrum chunk (images per order-2 pass) and, when the
-tensor-core form is asked for, whether that size's kernels run in it or in the
-plain FP32 form (the more precise of the two, so either meets the tensor-core
-form's bar), by timing candidates; the choice is cached per (N, J, L, form,
-batch bucket) in a JSON file.
+tensor-core form is asked for, which launch groups run their tensor-core
+kernel and which the plain FP32 kernel (the more precise of the two, so either
+meets the tensor-core form's bar), by timing candidates; the choices are
+cached per (N, J, L, form, batch bucket) in a JSON file.
 """
 import json
 import math
@@ -51,9 +51,10 @@ def _store_cache(entries):
 
 def autotune(module, batch, steps=3, candidates=None):
     """Time chunk sizes (images per order-2 pass) for ``module`` at ``batch``
-    images -- and, for a module in the tensor-core form, both kernel forms --
-    and keep the fastest; cached per (N, J, L, form, batch bucket).  Returns
-    the chosen chunk (the chosen form is left in ``module.tensor_cores``)."""
+    images and keep the fastest; for a module in the tensor-core form, then
+    time every launch group in its tensor-core and its plain kernel and keep
+    the faster per group (``module.set_group_tensor_cores``).  Cached per (N,
+    J, L, form, batch bucket).  Returns the chosen chunk."""
     from . import _lib
     form = 'tc' if module.tensor_cores else 'plain'
     bucket = 1 << max(0, math.ceil(math.log2(max(1, batch))))
@@ -62,7 +63,8 @@ def autotune(module, batch, steps=3, candidates=None):
         entries = _load_cache()
     if key in entries:
         module.set_chunk(entries[key]['chunk'])
-        module.tensor_cores = entries[key].get('tensor_cores', module.tensor_cores)
+        if 'tc_groups' in entries[key]:
+            module.set_group_tensor_cores(entries[key]['tc_groups'])
         return entries[key]['chunk']
     dev = module.tensor0.device
     plan = module._get_plan()
@@ -71,29 +73,37 @@ def autotune(module, batch, steps=3, candidates=None):
     if candidates is None:
         candidates = sorted({max(1, c) for c in (default // 4, default // 2, default, default * 2, batch)})
     x = torch.rand((batch,) + module.shape, device=dev)
-    forms = (True, False) if module.tensor_cores else (False,)
     best = None
     with torch.no_grad():
-        for tc in forms:
-            module.tensor_cores = tc
-            for c in candidates:
-                module.set_chunk(c)
+        for c in candidates:
+            module.set_chunk(c)
+            module(x)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(steps):
                 module(x)
-                torch.cuda.synchronize(dev)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                for _ in range(steps):
-                    module(x)
-                e1.record()
-                e1.synchronize()
-                ms = e0.elapsed_time(e1) / steps
-                if best is None or ms < best[1]:
-                    best = (c, ms, tc)
-    module.set_chunk(best[0])
-    module.tensor_cores = best[2]
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            if best is None or ms < best[1]:
+                best = (c, ms)
+        module.set_chunk(best[0])
+        entry = {'chunk': best[0], 'ms': best[1]}
+        if module.tensor_cores:
+            ng = lib.kym_s2d_group_count(plan.h)
+            module.set_group_tensor_cores([True] * ng)
+            module(x)
+            t_on = module.group_times(x, steps)
+            module.set_group_tensor_cores([False] * ng)
+            module(x)
+            t_off = module.group_times(x, steps)
+            mask = [a <= b for a, b in zip(t_on, t_off)]
+            module.set_group_tensor_cores(mask)
+            entry['tc_groups'] = mask
     with _CACHE_LOCK:
         entries = _load_cache()
-        entries[key] = {'chunk': best[0], 'ms': best[1], 'tensor_cores': best[2]}
+        entries[key] = entry
         _store_cache(entries)
     return best[0]
 

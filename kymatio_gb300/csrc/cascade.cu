@@ -226,6 +226,7 @@ struct Group {
   bool has_ct = false;   // a compile-time specialised variant exists
   CtEntry ct{};
   bool has_tc = false;   // a tensor-core variant exists (childless tasks only)
+  bool tc_on = true;     // kym_s2d_forward_tc uses it (kym_s2d_set_group_tc)
   size_t tc_smem = 0;
   TcLauncher tc = nullptr;
   TcLauncher tcdft = nullptr;     // DFT-GEMM tensor-core variant (childless tasks of the small sizes)
@@ -574,8 +575,8 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           cudaEventCreate(&e1);
           cudaEventRecord(e0, stream);
         }
-        if (a.lp && g.tcdft && a.opnd) err = g.tcdft(Li, F, *a.lp, a.status, ni, stream);
-        else if (a.lp && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
+        if (a.lp && g.tc_on && g.tcdft && a.opnd) err = g.tcdft(Li, F, *a.lp, a.status, ni, stream);
+        else if (a.lp && g.tc_on && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
         else if (g.lines) err = g.lines(Li, F, ni, stream);
         else if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
         else if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
@@ -1375,15 +1376,24 @@ extern "C" int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, floa
 extern "C" int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group) {
   if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
   const auto& g = plan->p.groups[group];
+  if (!g.tc_on) return 0;
   if (g.tcdft && kym::g_use_tcdft.load()) return 2;
   return g.has_tc ? 1 : 0;
+}
+
+extern "C" int kym_s2d_set_group_tc(kym_s2d_plan* plan, int group, int enable) {
+  if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
+  kym::Group& g = plan->p.groups[group];
+  const int prev = g.tc_on ? 1 : 0;
+  g.tc_on = enable != 0;
+  return prev;
 }
 
 extern "C" int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores) {
   if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
   const kym::Group& g = plan->p.groups[group];
-  if (tensor_cores && g.tcdft && kym::g_use_tcdft.load()) return 2;  // fold pass, GEMM kernel
-  if (tensor_cores && g.has_tc) return 1;
+  if (tensor_cores && g.tc_on && g.tcdft && kym::g_use_tcdft.load()) return 2;  // fold pass, GEMM kernel
+  if (tensor_cores && g.tc_on && g.has_tc) return 1;
   if (g.lines) return g.L.modulus ? 4 : 3;  // rows, columns, [rows + fold], low-pass
   return 1;
 }
@@ -1398,7 +1408,7 @@ extern "C" int kym_s2d_group_launches(const kym_s2d_plan* plan, int group, int b
   const int nch = (batch + chunk - 1) / chunk;
   chunk = (batch + nch - 1) / nch;
   const int k = kym_s2d_group_kernels(plan, group, tensor_cores);
-  const bool fused_tc = tensor_cores && (g.has_tc || (g.tcdft && kym::g_use_tcdft.load()));
+  const bool fused_tc = tensor_cores && g.tc_on && (g.has_tc || (g.tcdft && kym::g_use_tcdft.load()));
   auto sub = [&](int n) {
     if (!g.lines || fused_tc) return 1;
     const double slot_bytes = (double)g.tasks.size() * g.L.mr * g.L.mc * sizeof(float2);

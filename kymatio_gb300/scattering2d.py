@@ -207,6 +207,44 @@ class Scattering2D(nn.Module):
                                                ws.data_ptr(), ws_bytes, stream), 'kym_s2d_forward')
         return out
 
+    def group_times(self, x, steps=3):
+        """CUDA-event time (ms) of every launch group of the cascade in one
+        forward of x, averaged over ``steps`` forwards (profiling, autotuning)."""
+        import ctypes
+        plan, lib = self._get_plan(), _lib.load()
+        ng = lib.kym_s2d_group_count(plan.h)
+        gms = (ctypes.c_float * ng)()
+        B = x.shape[0]
+        acc = [0.0] * ng
+        with torch.cuda.device(x.device):
+            out = torch.empty((B, self._channels) + self._out_hw, dtype=torch.float32, device=x.device)
+            ptrs = self._filter_ptrs()
+            ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, B)
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=x.device)
+            stream = torch.cuda.current_stream(x.device).cuda_stream
+            for _ in range(steps):
+                if self.tensor_cores:
+                    lr, lc = self._lowpass_ptrs()
+                    _lib.check(lib.kym_s2d_forward_tc(plan.h, x.data_ptr(), out.data_ptr(), B, ptrs, self._n_filters,
+                                                      lr, lc, self.J, ws.data_ptr(), ws_bytes,
+                                                      self._tc_status.data_ptr(), stream, gms, ng),
+                               'kym_s2d_forward_tc')
+                else:
+                    _lib.check(lib.kym_s2d_forward_timed(plan.h, x.data_ptr(), out.data_ptr(), B, ptrs,
+                                                         self._n_filters, ws.data_ptr(), ws_bytes, stream, gms, ng),
+                               'kym_s2d_forward_timed')
+                acc = [a + gms[i] for i, a in enumerate(acc)]
+        return [a / steps for a in acc]
+
+    def set_group_tensor_cores(self, mask):
+        """In the tensor-core form, run launch group g in its tensor-core kernel
+        when mask[g] is true, else in the plain FP32 kernel (more precise, so
+        within the form's bar); the autotuner picks the mask by timing."""
+        plan, lib = self._get_plan(), _lib.load()
+        for g, on in enumerate(mask):
+            if lib.kym_s2d_set_group_tc(plan.h, g, int(bool(on))) < 0:
+                raise ValueError('no launch group %d' % g)
+
     def _backward_raw(self, x, grad):
         """grad_x = J^T grad through kym_s2d_backward (hand-written adjoints)."""
         plan = self._get_plan()

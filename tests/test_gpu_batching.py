@@ -65,10 +65,10 @@ def test_mixed_batch_outputs_not_aliased():
         assert torch.equal(first[s], keep[s])
 
 
-def test_autotune_picks_a_form_per_size(tmp_path, monkeypatch):
-    """In the tensor-core form the autotuner may keep a size in the plain
-    form (more precise); either way the results meet the tensor-core bar and
-    the choice is cached."""
+def test_autotune_picks_a_form_per_group(tmp_path, monkeypatch):
+    """In the tensor-core form the autotuner may keep launch groups in their
+    plain kernels (more precise); either way the results meet the tensor-core
+    bar and the choice is cached."""
     if not torch.cuda.is_available():
         pytest.skip('no CUDA device')
     monkeypatch.setenv('KYMATIO_GB300_CACHE', str(tmp_path))
@@ -81,7 +81,14 @@ def test_autotune_picks_a_form_per_size(tmp_path, monkeypatch):
     M = MixedScattering2D(list(xs), tensor_cores=True, tune=True).to(dev)
     out = M.forward_grouped(xs)
     entries = json.load(open(tmp_path / 'autotune.json'))
-    assert all('tensor_cores' in v for v in entries.values()) and len(entries) == 2
+    assert all('tc_groups' in v for v in entries.values()) and len(entries) == 2
+    for s, m in M.mods.items():
+        plan = m._get_plan()
+        from kymatio_gb300 import _lib
+        lib = _lib.load()
+        used = [lib.kym_s2d_group_uses_tc(plan.h, g) > 0 for g in range(lib.kym_s2d_group_count(plan.h))]
+        mask = entries[[k for k in entries if k.startswith('%sx%s/' % (s, s))][0]]['tc_groups']
+        assert all(u <= bool(b) for u, b in zip(used, mask))
     for s, x in xs.items():
         ref = Oracle(default_J(s), (s, s))(x.cpu().numpy().astype(np.float64))
         assert rel_l2(out[s].cpu().numpy(), ref) <= 5e-5
