@@ -466,6 +466,10 @@ def _extra_fwd_bwd_128(dev, flush, steps, warmup):
             'fwd_bwd_ms_recompute': fwdbwd_rc, 'ratio_recompute': fwdbwd_rc / fwd, 'cpu_baseline': cpu}
 
 
+#: input slices of the end-to-end host forward
+E2E_PARTS = 1
+
+
 def _lib_handle():
     from kymatio_gb300 import _lib
     return _lib.load()
@@ -716,18 +720,13 @@ def run_ours(args, world, rank, local):
     # ---- end to end through the public API (tensor-core form): pinned host in, host out
     S.tensor_cores = True
     out_host = torch.empty((BATCH, S._channels) + S._out_hw, dtype=torch.float32).pin_memory()
-    for _ in range(max(1, args.warmup)):
-        out_host.copy_(S(x_host.to(dev, non_blocking=True)), non_blocking=True)
-    torch.cuda.synchronize()
-    barrier(world)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        flush.zero_()
-        out_host.copy_(S(x_host.to(dev, non_blocking=True)), non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
+
+    def e2e_step(kind):
+        if kind == 'host':  # Scattering2D.forward_host: transfers overlapped with the cascade
+            S.forward_host(x_host, out_host, parts=args.e2e_parts, sync=False)
+        else:  # tensor API: copy in, forward, copy out, one after the other
+            out_host.copy_(S(x_host.to(dev, non_blocking=True)), non_blocking=True)
+
     fe0, fe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     fe0.record(stream)
     for _ in range(args.steps):
@@ -735,8 +734,23 @@ def run_ours(args, world, rank, local):
     fe1.record(stream)
     torch.cuda.synchronize()
     flush_ms = fe0.elapsed_time(fe1)
-    e2e_ms = max_over_ranks((e0.elapsed_time(e1) - flush_ms) / args.steps, world)
-    e2e = BATCH * world / (e2e_ms / 1e3)
+    e2e_ms = {}
+    for kind in ('tensor', 'host'):
+        for _ in range(max(1, args.warmup)):
+            e2e_step(kind)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            flush.zero_()
+            e2e_step(kind)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms[kind] = max_over_ranks((e0.elapsed_time(e1) - flush_ms) / args.steps, world)
+    e2e = BATCH * world / (e2e_ms['host'] / 1e3)
+    e2e_tensor = BATCH * world / (e2e_ms['tensor'] / 1e3)
     # ---- roofline of the dominant launch group of the tensor-core form -----------
     # (one launch = all the kernels of the group over one chunk of images)
     per_launch = [g_tc[g] / (1 if gi[0] == 0 else n_chunks) for g, gi in enumerate(ginfo)]
@@ -813,7 +827,11 @@ def run_ours(args, world, rank, local):
             'rel_l2_vs_fp64': prec.get('tc'), 'rel_l2_orders': ['S0', 'S1', 'S2'],
             'tc_status': tc_status,
             'e2e': {'value': e2e, 'unit': 'img/s', 'h2d_bytes_per_step': int(x_host.numel() * 4),
-                    'd2h_bytes_per_step': int(out_host.numel() * 4)},
+                    'd2h_bytes_per_step': int(out_host.numel() * 4),
+                    'api': 'Scattering2D.forward_host (kym_s2d_forward_host), pinned host buffers, input in '
+                           '%d slices, each group\'s channels copied back as it finishes' % args.e2e_parts,
+                    'tensor_api': {'value': e2e_tensor, 'unit': 'img/s',
+                                   'api': 'x_host.to(cuda) -> Scattering2D -> copy to pinned host, in sequence'}},
             'gpu_launches': launches_per_step * args.steps,
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm_peak, 'unit': 'GB/s',
                          'frac': achieved / hbm_peak, 'traffic': traffic,
@@ -860,6 +878,8 @@ def main():
                     help='comma-separated forms (plain, tc): run --repeat forwards of each on the benchmark batch '
                          '(--batch images) and exit; for ncu launch lists and captures')
     ap.add_argument('--repeat', type=int, default=3)
+    ap.add_argument('--e2e-parts', type=int, default=E2E_PARTS,
+                    help='input slices of the end-to-end host forward')
     args = ap.parse_args()
     global BATCH
     BATCH = args.batch

@@ -104,6 +104,23 @@ int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int
                        int n_filters, const float* const* lowpass_rows, const float* const* lowpass_cols,
                        int n_lowpass, void* workspace, size_t workspace_bytes, unsigned* status, void* stream,
                        float* group_ms, int max_groups);
+/* End-to-end forward between host buffers: x_host (batch, M, N) in,
+ * out_host (batch, C, out_rows, out_cols) out, through the caller's device
+ * buffers x_dev / out_dev of the same sizes.  The input is copied in `parts`
+ * slices on a copy stream of the plan and the input stage of each slice starts
+ * as it lands; each launch group's output channels are copied back on a second
+ * copy stream as soon as the group has finished, so the transfers overlap the
+ * cascade (host buffers page-locked; pageable ones give the same result
+ * without the overlap).  lowpass_rows / lowpass_cols / status as in
+ * kym_s2d_forward_tc select the tensor-core form; all three NULL the plain
+ * form.  Ordered on `stream`: work enqueued there after this call sees
+ * out_host complete.  No counterpart in the reference, whose frontend takes
+ * tensors on the module's device (kymatio/scattering2d/frontend/
+ * torch_frontend.py:72-111). */
+int kym_s2d_forward_host(const kym_s2d_plan* plan, const float* x_host, float* out_host, int batch,
+                         const float* const* filters, int n_filters, const float* const* lowpass_rows,
+                         const float* const* lowpass_cols, int n_lowpass, unsigned* status, float* x_dev,
+                         float* out_dev, void* workspace, size_t workspace_bytes, int parts, void* stream);
 /* Tensor-core form of launch group `group` in kym_s2d_forward_tc: 0 none
  * (FP32 kernel), 1 the low-pass product on tcgen05, 2 the DFT-GEMM form. */
 int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);

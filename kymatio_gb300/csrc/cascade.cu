@@ -236,6 +236,7 @@ struct Group {
   size_t smem = 0;
   bool oned = false;
   int level = 0;         // 0: input stage, 1: order 1, 2: order 2
+  std::vector<std::pair<int, int>> out_runs;  // output channels it writes, as runs [first, end)
 };
 
 int odd_pitch(int n) { return (n % 2 == 0) ? n + 1 : n; }
@@ -250,6 +251,7 @@ struct DeviceState {
   float2* tw = nullptr;
   BwdTask* btasks = nullptr;
   GatherItem* gather = nullptr;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;  // host transfers of kym_s2d_forward_host
 };
 
 // Backward launch group: mirrors one forward group's geometry.
@@ -277,6 +279,11 @@ struct CascadePlan {
   size_t opnd_bytes = 0;                      // per image: DFT-GEMM operand slots of the largest such group
   int chunk = 0;
   std::vector<Group> groups;
+  // launch order of the groups: the input stage, the order-1 groups that
+  // store parent spectra, the order-2 groups, then the childless order-1
+  // groups (they depend on nothing later, and a short group last leaves
+  // little output to copy after the cascade in kym_s2d_forward_host)
+  std::vector<int> order;
   std::vector<Task> all_tasks;
   // backward
   std::vector<BwdGroup> bgroups;
@@ -300,11 +307,18 @@ struct CascadePlan {
       cudaFree(kv.second.tw);
       cudaFree(kv.second.btasks);
       cudaFree(kv.second.gather);
+      if (kv.second.copy_in) cudaStreamDestroy(kv.second.copy_in);
+      if (kv.second.copy_out) cudaStreamDestroy(kv.second.copy_out);
     }
     if (have) cudaSetDevice(cur);
     cudaGetLastError();
   }
 };
+
+static int fail_cuda(cudaError_t e, const char* what) {
+  set_error_message(what, cudaGetErrorString(e));
+  return KYM_ERR_CUDA;
+}
 
 // Host-side finalisation: task offsets into one concatenated table.
 static int finalize_groups(CascadePlan* P) {
@@ -333,6 +347,53 @@ static int finalize_groups(CascadePlan* P) {
   P->u1_elems += P->u1_elems & 1;
   P->all_tasks.clear();
   for (auto& g : P->groups) P->all_tasks.insert(P->all_tasks.end(), g.tasks.begin(), g.tasks.end());
+  // output channel runs, and the launch order
+  for (auto& g : P->groups) {
+    std::vector<int> ch;
+    for (const Task& t : g.tasks)
+      if (t.out_ch >= 0) ch.push_back(t.out_ch);
+    std::sort(ch.begin(), ch.end());
+    ch.erase(std::unique(ch.begin(), ch.end()), ch.end());
+    g.out_runs.clear();
+    for (size_t i = 0; i < ch.size(); ++i) {
+      if (!g.out_runs.empty() && g.out_runs.back().second == ch[i]) ++g.out_runs.back().second;
+      else g.out_runs.push_back({ch[i], ch[i] + 1});
+    }
+  }
+  auto childless = [](const Group& g) {
+    for (const Task& t : g.tasks)
+      if (t.dst_off >= 0) return false;
+    return true;
+  };
+  P->order.clear();
+  for (int cls = 0; cls < 4; ++cls)
+    for (size_t i = 0; i < P->groups.size(); ++i) {
+      const Group& g = P->groups[i];
+      const int c = g.level == 0 ? 0 : g.level == 2 ? 2 : (g.level == 1 && childless(g)) ? 3 : 1;
+      if (c == cls) P->order.push_back((int)i);
+    }
+  return KYM_OK;
+}
+
+// The two copy streams of kym_s2d_forward_host on the current device
+// (created on first use; the plan's device tables must exist already).
+static int host_copy_streams(CascadePlan* P, cudaStream_t* in, cudaStream_t* out) {
+  int d = 0;
+  cudaError_t e = cudaGetDevice(&d);
+  if (e != cudaSuccess) return fail_cuda(e, "host forward");
+  std::lock_guard<std::mutex> lock(P->mu);
+  auto it = P->dev.find(d);
+  if (it == P->dev.end()) {
+    set_error_message("host forward", "plan tables missing on this device");
+    return KYM_ERR_INVALID;
+  }
+  DeviceState& s = it->second;
+  if (!s.copy_in && (e = cudaStreamCreateWithFlags(&s.copy_in, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail_cuda(e, "copy stream");
+  if (!s.copy_out && (e = cudaStreamCreateWithFlags(&s.copy_out, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail_cuda(e, "copy stream");
+  *in = s.copy_in;
+  *out = s.copy_out;
   return KYM_OK;
 }
 
@@ -474,12 +535,28 @@ struct RunArgs {
   int max_groups = 0;
   float2* ysave = nullptr;  // non-null: every path stores its modulus input (per image gy2 + gy1 elements)
   unsigned char* opnd = nullptr;  // DFT-GEMM operand slots (chunk images)
+  // host transfers (kym_s2d_forward_host): the input is copied from x_host to
+  // the device input in `parts` slices on copy_in, each output channel run is
+  // copied to out_host on copy_out once the group writing it has finished
+  const float* x_host = nullptr;
+  float* out_host = nullptr;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  int parts = 1;
 };
 
-static int fail_cuda(cudaError_t e, const char* what) {
-  set_error_message(what, cudaGetErrorString(e));
-  return KYM_ERR_CUDA;
-}
+// Events of one host forward, destroyed when it returns (a recorded event may
+// be destroyed before it completes; waits already enqueued on it stand).
+struct EventPool {
+  std::vector<cudaEvent_t> ev;
+  cudaError_t make(cudaEvent_t* e) {
+    const cudaError_t r = cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+    if (r == cudaSuccess) ev.push_back(*e);
+    return r;
+  }
+  ~EventPool() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+};
 
 static int make_filter_table(CascadePlan* P, const float* const* filters, int nfilters, FilterTable* F) {
   if (!filters || nfilters != (int)P->filter_rows.size() || nfilters > kMaxFilters) {
@@ -512,9 +589,41 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
   const bool timed = a.group_ms && a.max_groups > 0;
   if (timed)
     for (int i = 0; i < a.max_groups; ++i) a.group_ms[i] = 0.f;
+  // host transfers: input slices [part0[p], part0[p + 1]) copied on copy_in
+  const bool hio = a.x_host && a.out_host && a.copy_in && a.copy_out;
+  EventPool pool;
+  const int parts = hio ? std::max(1, std::min(a.parts, batch)) : 1;
+  std::vector<int> part0(parts + 1);
+  for (int p = 0; p <= parts; ++p) part0[p] = (int)((long long)batch * p / parts);
+  std::vector<cudaEvent_t> in_ev(parts, nullptr);
+  int waited = 0;  // input slices `stream` already waits for
+  if (hio) {
+    // the copies start after the work already on `stream` (earlier users of
+    // the device input and the host output)
+    cudaEvent_t start;
+    if ((err = pool.make(&start)) != cudaSuccess || (err = cudaEventRecord(start, stream)) != cudaSuccess ||
+        (err = cudaStreamWaitEvent(a.copy_in, start, 0)) != cudaSuccess ||
+        (err = cudaStreamWaitEvent(a.copy_out, start, 0)) != cudaSuccess)
+      return fail_cuda(err, "host forward");
+    for (int p = 0; p < parts; ++p) {
+      const size_t off = (size_t)part0[p] * x_stride;
+      const size_t bytes = (size_t)(part0[p + 1] - part0[p]) * x_stride * sizeof(float);
+      if ((err = cudaMemcpyAsync(const_cast<float*>(x) + off, a.x_host + off, bytes, cudaMemcpyHostToDevice,
+                                 a.copy_in)) != cudaSuccess ||
+          (err = pool.make(&in_ev[p])) != cudaSuccess || (err = cudaEventRecord(in_ev[p], a.copy_in)) != cudaSuccess)
+        return fail_cuda(err, "host input copy");
+    }
+  }
+  // make `stream` wait for the input slices that hold images below `end`
+  auto wait_inputs = [&](int end) -> cudaError_t {
+    cudaError_t r = cudaSuccess;
+    while (hio && waited < parts && part0[waited] < end && r == cudaSuccess)
+      r = cudaStreamWaitEvent(stream, in_ev[waited++], 0);
+    return r;
+  };
   for (int c0 = 0; c0 < batch; c0 += chunk) {
     const int nimg = std::min(chunk, batch - c0);
-    for (size_t gi = 0; gi < P->groups.size(); ++gi) {
+    for (int gi : P->order) {
       const Group& g = P->groups[gi];
       if (g.level == 0 && c0 != 0 && !a.stage0_per_chunk) continue;  // input stage once over the batch
       CascadeLaunch L = g.L;
@@ -562,9 +671,17 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
         const double slot_bytes = (double)g.tasks.size() * g.L.mr * g.L.mc * sizeof(float2);
         step = (int)std::max(1.0, std::min(65535.0, 64.0 * 1024 * 1024 / slot_bytes));
       }
-      for (int i0 = 0; i0 < n; i0 += step) {
+      for (int i0 = 0; i0 < n;) {
         CascadeLaunch Li = L;
-        const int ni = std::min(step, n - i0);
+        int ni = std::min(step, n - i0);
+        if (hio && g.level == 0) {
+          // the input stage runs slice by slice as the slices land
+          const int first = L.img0 + i0;
+          int p = 0;
+          while (part0[p + 1] <= first) ++p;
+          ni = std::min(ni, part0[p + 1] - first);
+          if ((err = wait_inputs(first + ni)) != cudaSuccess) return fail_cuda(err, "host forward");
+        }
         Li.img0 = L.img0 + i0;
         if (Li.src) Li.src = L.src + (size_t)i0 * L.src_stride;
         if (Li.dst) Li.dst = L.dst + (size_t)i0 * L.dst_stride;
@@ -593,8 +710,32 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           }
           return fail_cuda(err, "cascade launch");
         }
+        i0 += ni;
+      }
+      if (hio && !g.out_runs.empty()) {
+        // this group's channels are final for its images: copy them out
+        const int a0 = g.level == 0 ? L.img0 : c0;
+        cudaEvent_t done;
+        if ((err = pool.make(&done)) != cudaSuccess || (err = cudaEventRecord(done, stream)) != cudaSuccess ||
+            (err = cudaStreamWaitEvent(a.copy_out, done, 0)) != cudaSuccess)
+          return fail_cuda(err, "host forward");
+        const size_t plane = (size_t)P->out_nr * P->out_nc;
+        for (const auto& r : g.out_runs) {
+          const size_t off = (size_t)a0 * out_stride + r.first * plane;
+          err = cudaMemcpy2DAsync(a.out_host + off, out_stride * sizeof(float), out + off, out_stride * sizeof(float),
+                                  (size_t)(r.second - r.first) * plane * sizeof(float), n, cudaMemcpyDeviceToHost,
+                                  a.copy_out);
+          if (err != cudaSuccess) return fail_cuda(err, "host output copy");
+        }
       }
     }
+  }
+  if (hio) {
+    // `stream` orders after every copy: later work on it sees out_host complete
+    cudaEvent_t fin;
+    if ((err = wait_inputs(batch)) != cudaSuccess || (err = pool.make(&fin)) != cudaSuccess ||
+        (err = cudaEventRecord(fin, a.copy_out)) != cudaSuccess || (err = cudaStreamWaitEvent(stream, fin, 0)) != cudaSuccess)
+      return fail_cuda(err, "host forward");
   }
   if (timed) {
     cudaError_t se = cudaStreamSynchronize(stream);
@@ -612,7 +753,8 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
 static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const float* const* filters,
                     int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
                     float* group_ms = nullptr, int max_groups = 0, const LowpassTable* lp = nullptr,
-                    unsigned* status = nullptr, float2* ysave = nullptr) {
+                    unsigned* status = nullptr, float2* ysave = nullptr, const float* x_host = nullptr,
+                    float* out_host = nullptr, int parts = 1) {
   if (!P || !x || !out || batch < 0) {
     set_error_message("forward", "null plan, input or output");
     return KYM_ERR_INVALID;
@@ -647,6 +789,17 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   a.status = status;
   a.ysave = ysave;
   if (dft) a.opnd = static_cast<unsigned char*>(workspace) + opnd_off;
+  if (x_host || out_host) {
+    if (!x_host || !out_host) {
+      set_error_message("host forward", "null host input or output");
+      return KYM_ERR_INVALID;
+    }
+    rc = host_copy_streams(P, &a.copy_in, &a.copy_out);
+    if (rc) return rc;
+    a.x_host = x_host;
+    a.out_host = out_host;
+    a.parts = parts;
+  }
   return run_core(P, x, out, batch, F, a, stream);
 }
 
@@ -1371,6 +1524,31 @@ extern "C" int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, floa
   return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x, out, batch, filters, n_filters, workspace,
                        workspace_bytes, static_cast<cudaStream_t>(stream), group_ms, group_ms ? max_groups : 0, &lp,
                        status);
+}
+
+extern "C" int kym_s2d_forward_host(const kym_s2d_plan* plan, const float* x_host, float* out_host, int batch,
+                                    const float* const* filters, int n_filters, const float* const* lowpass_rows,
+                                    const float* const* lowpass_cols, int n_lowpass, unsigned* status, float* x_dev,
+                                    float* out_dev, void* workspace, size_t workspace_bytes, int parts,
+                                    void* stream) {
+  if (!plan || !x_host || !out_host || !x_dev || !out_dev || parts < 1) {
+    kym::set_error_message("forward_host", "null plan, host or device buffer, or parts < 1");
+    return KYM_ERR_INVALID;
+  }
+  const bool tc = lowpass_rows || lowpass_cols || status;
+  if (tc && (!lowpass_rows || !lowpass_cols || !status || n_lowpass < 1 || n_lowpass > kym::kMaxLowpass)) {
+    kym::set_error_message("forward_host", "the tensor-core form needs the low-pass factors and a status word");
+    return KYM_ERR_INVALID;
+  }
+  kym::LowpassTable lp;
+  std::memset(&lp, 0, sizeof(lp));
+  for (int i = 0; tc && i < n_lowpass; ++i) {
+    lp.r[i] = lowpass_rows[i];
+    lp.c[i] = lowpass_cols[i];
+  }
+  return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x_dev, out_dev, batch, filters, n_filters, workspace,
+                       workspace_bytes, static_cast<cudaStream_t>(stream), nullptr, 0, tc ? &lp : nullptr,
+                       tc ? status : nullptr, nullptr, x_host, out_host, parts);
 }
 
 extern "C" int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group) {

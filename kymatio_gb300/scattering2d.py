@@ -207,6 +207,52 @@ class Scattering2D(nn.Module):
                                                ws.data_ptr(), ws_bytes, stream), 'kym_s2d_forward')
         return out
 
+    def forward_host(self, x, out=None, parts=1, sync=True):
+        """End-to-end forward between host tensors: x a CPU float32 tensor
+        (..., M, N), returns (..., C, m, n) on the host (in ``out``, or a new
+        page-locked tensor).  The input goes to the module's device in
+        ``parts`` slices and each launch group's channels come back as soon as
+        the group has finished (kym_s2d_forward_host), so the transfers
+        overlap the cascade; page-locked inputs (``x.pin_memory()``) overlap
+        best.  Tensor-core form when ``tensor_cores``.  With ``sync=False`` the
+        call returns once the work is queued on the current stream:
+        synchronise before reading the result."""
+        if not torch.is_tensor(x) or x.is_cuda or x.dtype != torch.float32 or not x.is_contiguous():
+            raise TypeError('forward_host takes a contiguous float32 CPU tensor.')
+        hw = (self._M_padded, self._N_padded) if self.pre_pad else self.shape
+        if len(x.shape) < 2 or tuple(x.shape[-2:]) != hw:
+            raise RuntimeError('Tensor must be of spatial size (%i,%i).' % hw)
+        dev = self.tensor0.device
+        if dev.type != 'cuda':
+            raise TypeError('The module must be on a CUDA device: the GB300 scattering engine runs on CUDA only.')
+        plan, lib = self._get_plan(), _lib.load()
+        xb = x.reshape((-1,) + hw)
+        B = xb.shape[0]
+        shape = tuple(x.shape[:-2]) + (self._channels,) + self._out_hw
+        if out is None:
+            out = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+        elif out.is_cuda or out.dtype != torch.float32 or not out.is_contiguous() or tuple(out.shape) != shape:
+            raise TypeError('out must be a contiguous float32 CPU tensor of shape %s.' % (shape,))
+        if B == 0:
+            return out
+        with torch.cuda.device(dev):
+            x_dev = torch.empty((B,) + hw, dtype=torch.float32, device=dev)
+            out_dev = torch.empty((B, self._channels) + self._out_hw, dtype=torch.float32, device=dev)
+            ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, B)
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+            stream = torch.cuda.current_stream(dev).cuda_stream
+            lr = lc = status = None
+            if self.tensor_cores:
+                lr, lc = self._lowpass_ptrs()
+                status = self._tc_status.data_ptr()
+            _lib.check(lib.kym_s2d_forward_host(plan.h, xb.data_ptr(), out.data_ptr(), B, self._filter_ptrs(),
+                                                self._n_filters, lr, lc, self.J, status, x_dev.data_ptr(),
+                                                out_dev.data_ptr(), ws.data_ptr(), ws_bytes, int(parts), stream),
+                       'kym_s2d_forward_host')
+            if sync:
+                torch.cuda.current_stream(dev).synchronize()
+        return out
+
     def group_times(self, x, steps=3):
         """CUDA-event time (ms) of every launch group of the cascade in one
         forward of x, averaged over ``steps`` forwards (profiling, autotuning)."""
