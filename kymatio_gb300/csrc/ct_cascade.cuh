@@ -84,6 +84,54 @@ __device__ __forceinline__ void ct_load(float2* A, const CascadeLaunch& L, const
     const float4* src4 = reinterpret_cast<const float4*>(L.src + (size_t)img * L.src_stride + t.src_off);
     const float2* psi2 = reinterpret_cast<const float2*>(F.f[t.psi]);
     const float sc = L.load_scale;
+    if constexpr (!ONED && C == 1 && MR % 2 == 0) {
+      // The source is the spectrum of a real image, P x Q = KF MR x KF MC:
+      // X[P - r][(Q - c) % Q] = conj X[r][c].  The aliases of row u' = MR - u
+      // are the mirrors of row u's, (r, c) = (u + a MR, v + b MC), so one pass
+      // over row u's source values also gives
+      //   Y[u'][(MC - v) % MC] = sum conj X[r][c] psi[P - r][(Q - c) % Q]
+      // (and column v + 1 -> MC - 1 - v): half the source loads per output.
+      // Rows 0 and MR / 2 are their own mirrors and are folded directly.
+      constexpr int HC = MC / 2, NI = (MR / 2 + 1) * HC, P = KF * MR;
+      const float* psi = F.f[t.psi];
+#pragma unroll 2
+      for (int e = threadIdx.x; e < NI; e += NT) {
+        const int u = e / HC, v = 2 * (e % HC);
+        const bool pair = u != 0 && u != MR / 2;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f), accp = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int a = 0; a < KF; ++a) {
+          const int r = u + a * MR;
+#pragma unroll
+          for (int b = 0; b < KF; ++b) {
+            const int c = v + b * MC;
+            const size_t half = ((size_t)r * SCOLS + c) >> 1;
+            const float4 s4 = __ldg(src4 + half);
+            const float2 f2 = __ldg(psi2 + half);
+            acc.x = fmaf(s4.x, f2.x, acc.x);
+            acc.y = fmaf(s4.y, f2.x, acc.y);
+            acc.z = fmaf(s4.z, f2.y, acc.z);
+            acc.w = fmaf(s4.w, f2.y, acc.w);
+            if (pair) {
+              const float* prow = psi + (size_t)(P - r) * SCOLS;
+              const float g0 = __ldg(prow + (c == 0 ? 0 : SCOLS - c));
+              const float g1 = __ldg(prow + (SCOLS - 1 - c));
+              accp.x = fmaf(s4.x, g0, accp.x);
+              accp.y = fmaf(-s4.y, g0, accp.y);
+              accp.z = fmaf(s4.z, g1, accp.z);
+              accp.w = fmaf(-s4.w, g1, accp.w);
+            }
+          }
+        }
+        *at(u, v) = make_float2(acc.x * sc, acc.y * sc);
+        *at(u, v + 1) = make_float2(acc.z * sc, acc.w * sc);
+        if (pair) {
+          *at(MR - u, (MC - v) % MC) = make_float2(accp.x * sc, accp.y * sc);
+          *at(MR - u, MC - 1 - v) = make_float2(accp.z * sc, accp.w * sc);
+        }
+      }
+      return;
+    }
 #pragma unroll 2
     for (int e = threadIdx.x; e < NLOC / 2; e += NT) {
       const int u = (2 * e) / MC, v = (2 * e) % MC;
