@@ -47,6 +47,16 @@ int kym_set_specialized(int enable);
  * reference (a form of kymatio/scattering2d/core/scattering2d.py:48-75). */
 int kym_set_tc_dft(int enable);
 
+/* Forwards after this call run the launch groups that do not depend on the
+ * heaviest order-1 scale (the other order-1 scales and their order-2 groups)
+ * on a low-priority side stream of the plan, forked from and joined back to
+ * the caller's stream around every chunk, so that their blocks fill the SMs
+ * the main chain leaves idle (enable=1, the default), or every group on the
+ * caller's stream (enable=0).  Results are identical either way.  Timed
+ * forwards and the DFT-GEMM form run on one stream.  Returns the previous
+ * setting.  No counterpart in the reference. */
+int kym_set_side_lane(int enable);
+
 /* ------------------------------------------------------------------------
  * 2-D scattering (replaces the forward of ScatteringTorch2D,
  * kymatio/scattering2d/frontend/torch_frontend.py:72-111, driving

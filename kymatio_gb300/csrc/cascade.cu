@@ -237,11 +237,13 @@ struct Group {
   bool oned = false;
   int level = 0;         // 0: input stage, 1: order 1, 2: order 2
   std::vector<std::pair<int, int>> out_runs;  // output channels it writes, as runs [first, end)
+  int lane = 0;          // 0: the caller's stream, 1: the plan's side stream
 };
 
 int odd_pitch(int n) { return (n % 2 == 0) ? n + 1 : n; }
 std::atomic<bool> g_use_ct{true};
 std::atomic<bool> g_use_tcdft{false};
+std::atomic<bool> g_use_side{true};
 int swz_len(int n) { return n + (n >> 4) + 1; }
 
 }  // namespace
@@ -252,6 +254,7 @@ struct DeviceState {
   BwdTask* btasks = nullptr;
   GatherItem* gather = nullptr;
   cudaStream_t copy_in = nullptr, copy_out = nullptr;  // host transfers of kym_s2d_forward_host
+  cudaStream_t side = nullptr;  // low-priority lane of the forward's independent group chains
 };
 
 // Backward launch group: mirrors one forward group's geometry.
@@ -309,6 +312,7 @@ struct CascadePlan {
       cudaFree(kv.second.gather);
       if (kv.second.copy_in) cudaStreamDestroy(kv.second.copy_in);
       if (kv.second.copy_out) cudaStreamDestroy(kv.second.copy_out);
+      if (kv.second.side) cudaStreamDestroy(kv.second.side);
     }
     if (have) cudaSetDevice(cur);
     cudaGetLastError();
@@ -331,13 +335,14 @@ static int finalize_groups(CascadePlan* P) {
     total += g.tasks.size();
   }
   // the folded low-pass blocks of a line-split order-1 group sit after each
-  // image's parent spectra (groups run one after the other: one region)
+  // image's parent spectra, one region per such group (groups of different
+  // launch lanes may run at the same time)
   long long lp = 0;
   for (auto& g : P->groups) {
     g.L.bsum_off = -1;
     if (g.lines && g.L.modulus && g.level == 1) {
-      g.L.bsum_off = P->u1_elems;
-      lp = std::max(lp, (long long)g.tasks.size() * g.L.sr * g.L.sc);
+      g.L.bsum_off = P->u1_elems + lp;
+      lp += (long long)g.tasks.size() * g.L.sr * g.L.sc;
     }
   }
   P->u1_elems += lp;
@@ -365,6 +370,47 @@ static int finalize_groups(CascadePlan* P) {
       if (t.dst_off >= 0) return false;
     return true;
   };
+  // launch lanes: an order-1 group and the order-2 groups reading its parent
+  // spectra form a chain; the heaviest chain runs on the caller's stream,
+  // the others on a low-priority side stream, where their blocks fill the
+  // SMs the first chain leaves idle (its tails and narrow launches)
+  {
+    const int ng = (int)P->groups.size();
+    std::vector<int> chain(ng, -1);
+    for (int i = 0; i < ng; ++i)
+      if (P->groups[i].level == 1) chain[i] = i;
+    for (int i = 0; i < ng; ++i) {
+      const Group& g = P->groups[i];
+      if (g.level != 2 || g.tasks.empty()) continue;
+      const long long src = g.tasks[0].src_off;
+      for (int k = 0; k < ng && chain[i] < 0; ++k)
+        if (P->groups[k].level == 1)
+          for (const Task& t : P->groups[k].tasks)
+            if (t.dst_off == src) {
+              chain[i] = k;
+              break;
+            }
+    }
+    std::vector<double> weight(ng, 0.0);
+    for (int i = 0; i < ng; ++i) {
+      const Group& g = P->groups[i];
+      if (chain[i] < 0) continue;
+      const double area = (double)g.L.mr * g.L.mc;
+      weight[chain[i]] += (double)g.tasks.size() * area * (std::log2(std::max(2.0, area)) + g.L.kr * g.L.kc);
+    }
+    int heavy = -1;
+    for (int i = 0; i < ng; ++i)
+      if (P->groups[i].level == 1 && (heavy < 0 || weight[i] > weight[heavy])) heavy = i;
+    for (int i = 0; i < ng; ++i) {
+      Group& g = P->groups[i];
+      g.lane = (chain[i] >= 0 && chain[i] != heavy) ? 1 : 0;
+    }
+    for (int i = 0; i < ng; ++i)
+      if (P->groups[i].level == 2 && chain[i] < 0) {
+        for (auto& g : P->groups) g.lane = 0;  // unknown dependencies: one lane
+        break;
+      }
+  }
   P->order.clear();
   for (int cls = 0; cls < 4; ++cls)
     for (size_t i = 0; i < P->groups.size(); ++i) {
@@ -372,6 +418,29 @@ static int finalize_groups(CascadePlan* P) {
       const int c = g.level == 0 ? 0 : g.level == 2 ? 2 : (g.level == 1 && childless(g)) ? 3 : 1;
       if (c == cls) P->order.push_back((int)i);
     }
+  return KYM_OK;
+}
+
+// The side lane of the forward on the current device (created on first use,
+// lowest priority; the plan's device tables must exist already).
+static int side_stream(CascadePlan* P, cudaStream_t* side) {
+  int d = 0;
+  cudaError_t e = cudaGetDevice(&d);
+  if (e != cudaSuccess) return fail_cuda(e, "side stream");
+  std::lock_guard<std::mutex> lock(P->mu);
+  auto it = P->dev.find(d);
+  if (it == P->dev.end()) {
+    set_error_message("side stream", "plan tables missing on this device");
+    return KYM_ERR_INVALID;
+  }
+  DeviceState& s = it->second;
+  if (!s.side) {
+    int lo = 0, hi = 0;
+    if ((e = cudaDeviceGetStreamPriorityRange(&lo, &hi)) != cudaSuccess ||
+        (e = cudaStreamCreateWithPriority(&s.side, cudaStreamNonBlocking, lo)) != cudaSuccess)
+      return fail_cuda(e, "side stream");
+  }
+  *side = s.side;
   return KYM_OK;
 }
 
@@ -542,6 +611,9 @@ struct RunArgs {
   float* out_host = nullptr;
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
   int parts = 1;
+  // non-null: groups of lane 1 run here, forked from and joined back to the
+  // caller's stream around every chunk
+  cudaStream_t side = nullptr;
 };
 
 // Events of one host forward, destroyed when it returns (a recorded event may
@@ -623,9 +695,20 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
   };
   for (int c0 = 0; c0 < batch; c0 += chunk) {
     const int nimg = std::min(chunk, batch - c0);
+    bool forked = false;
     for (int gi : P->order) {
       const Group& g = P->groups[gi];
       if (g.level == 0 && c0 != 0 && !a.stage0_per_chunk) continue;  // input stage once over the batch
+      if (a.side && g.level > 0 && !forked) {
+        // the side lane starts once this chunk's inputs are ready: after
+        // the work already on the caller's stream (input stage, earlier chunks)
+        cudaEvent_t f;
+        if ((err = pool.make(&f)) != cudaSuccess || (err = cudaEventRecord(f, stream)) != cudaSuccess ||
+            (err = cudaStreamWaitEvent(a.side, f, 0)) != cudaSuccess)
+          return fail_cuda(err, "side lane fork");
+        forked = true;
+      }
+      const cudaStream_t gs = (a.side && g.lane == 1) ? a.side : stream;
       CascadeLaunch L = g.L;
       L.tasks = ds->tasks + g.task_off;
       L.ntasks = (int)g.tasks.size();
@@ -690,17 +773,17 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
         if (timed && (int)gi < a.max_groups) {
           cudaEventCreate(&e0);
           cudaEventCreate(&e1);
-          cudaEventRecord(e0, stream);
+          cudaEventRecord(e0, gs);
         }
-        if (a.lp && g.tc_on && g.tcdft && a.opnd) err = g.tcdft(Li, F, *a.lp, a.status, ni, stream);
-        else if (a.lp && g.tc_on && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, stream);
-        else if (g.lines) err = g.lines(Li, F, ni, stream);
-        else if (g.has_ct) err = g.ct.fn(Li, F, ni, stream);
-        else if (g.oned) err = launch_group<false, true>(g, Li, F, ni, stream);
-        else if (Li.cluster > 1) err = launch_group<true, false>(g, Li, F, ni, stream);
-        else err = launch_group<false, false>(g, Li, F, ni, stream);
+        if (a.lp && g.tc_on && g.tcdft && a.opnd) err = g.tcdft(Li, F, *a.lp, a.status, ni, gs);
+        else if (a.lp && g.tc_on && g.has_tc) err = g.tc(Li, F, *a.lp, a.status, ni, gs);
+        else if (g.lines) err = g.lines(Li, F, ni, gs);
+        else if (g.has_ct) err = g.ct.fn(Li, F, ni, gs);
+        else if (g.oned) err = launch_group<false, true>(g, Li, F, ni, gs);
+        else if (Li.cluster > 1) err = launch_group<true, false>(g, Li, F, ni, gs);
+        else err = launch_group<false, false>(g, Li, F, ni, gs);
         if (e0) {
-          cudaEventRecord(e1, stream);
+          cudaEventRecord(e1, gs);
           evs.push_back({(int)gi, {e0, e1}});
         }
         if (err != cudaSuccess) {
@@ -716,7 +799,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
         // this group's channels are final for its images: copy them out
         const int a0 = g.level == 0 ? L.img0 : c0;
         cudaEvent_t done;
-        if ((err = pool.make(&done)) != cudaSuccess || (err = cudaEventRecord(done, stream)) != cudaSuccess ||
+        if ((err = pool.make(&done)) != cudaSuccess || (err = cudaEventRecord(done, gs)) != cudaSuccess ||
             (err = cudaStreamWaitEvent(a.copy_out, done, 0)) != cudaSuccess)
           return fail_cuda(err, "host forward");
         const size_t plane = (size_t)P->out_nr * P->out_nc;
@@ -728,6 +811,13 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           if (err != cudaSuccess) return fail_cuda(err, "host output copy");
         }
       }
+    }
+    if (forked) {
+      // join: the next chunk reuses the parent-spectrum workspace
+      cudaEvent_t jn;
+      if ((err = pool.make(&jn)) != cudaSuccess || (err = cudaEventRecord(jn, a.side)) != cudaSuccess ||
+          (err = cudaStreamWaitEvent(stream, jn, 0)) != cudaSuccess)
+        return fail_cuda(err, "side lane join");
     }
   }
   if (hio) {
@@ -789,6 +879,18 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
   a.status = status;
   a.ysave = ysave;
   if (dft) a.opnd = static_cast<unsigned char*>(workspace) + opnd_off;
+  // independent group chains on the side lane (not while timing groups one
+  // by one, nor with the DFT-GEMM form, whose groups share operand slots)
+  bool lanes = g_use_side.load() && !group_ms && !a.opnd;
+  if (lanes) {
+    bool any = false;
+    for (const Group& g : P->groups) any |= g.lane == 1;
+    lanes = any;
+  }
+  if (lanes) {
+    rc = side_stream(P, &a.side);
+    if (rc) return rc;
+  }
   if (x_host || out_host) {
     if (!x_host || !out_host) {
       set_error_message("host forward", "null host input or output");
@@ -1442,6 +1544,10 @@ fail:
 
 extern "C" int kym_set_specialized(int enable) {
   return kym::g_use_ct.exchange(enable != 0) ? 1 : 0;
+}
+
+extern "C" int kym_set_side_lane(int enable) {
+  return kym::g_use_side.exchange(enable != 0) ? 1 : 0;
 }
 
 extern "C" int kym_set_tc_dft(int enable) {

@@ -62,3 +62,26 @@ def test_errors(dev):
     with pytest.raises(TypeError):
         S.forward_host(torch.zeros(2, 32, 32), out=torch.zeros(2, 3))
     assert S.forward_host(torch.zeros(0, 32, 32)).shape[0] == 0
+
+
+@pytest.mark.parametrize('J,side,chunk', [(3, 256, None), (4, 128, 3)])
+def test_side_lane_identical(dev, J, side, chunk):
+    """The side lane (independent group chains on a second stream) changes
+    nothing in the results, in either form, with several chunks too."""
+    from kymatio_gb300 import Scattering2D, _lib
+    lib = _lib.load()
+    S = Scattering2D(J, (side, side)).to(dev)
+    if chunk:
+        S.set_chunk(chunk)
+    x = torch.from_numpy(np.random.default_rng(J).random((7, side, side)).astype(np.float32)).to(dev)
+    for tc in (False, True):
+        S.tensor_cores = tc
+        prev = lib.kym_set_side_lane(0)
+        try:
+            one = S(x)
+            lib.kym_set_side_lane(1)
+            two = S(x)
+            torch.cuda.synchronize()
+        finally:
+            lib.kym_set_side_lane(prev)
+        assert torch.equal(one, two)
