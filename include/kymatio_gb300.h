@@ -143,7 +143,8 @@ int kym_s2d_set_group_tc(kym_s2d_plan* plan, int group, int enable);
 /* Kernels that group `group` launches per chunk of images: 1 for a fused
  * cascade kernel; 3 or 4 for the line-split passes of the sizes above one
  * CTA, per sub-launch (a sub-launch covers as many images as keep the
- * group's spectrum slots within 64 MiB) (tensor_cores != 0: in
+ * group's spectrum slots within 64 MiB; with several sub-launches the
+ * low-pass kernel runs once after them) (tensor_cores != 0: in
  * kym_s2d_forward_tc).  No counterpart in the reference (profiling). */
 int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores);
 /* Kernel launches of group `group` in one forward over `batch` images (its

@@ -754,8 +754,12 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
         const double slot_bytes = (double)g.tasks.size() * g.L.mr * g.L.mc * sizeof(float2);
         step = (int)std::max(1.0, std::min(65535.0, 64.0 * 1024 * 1024 / slot_bytes));
       }
+      // a line-split group runs its low-pass kernel once after all its
+      // sub-launches: one wide launch instead of one narrow one per sub-launch
+      const bool lp_after = g.lines && step < n;
       for (int i0 = 0; i0 < n;) {
         CascadeLaunch Li = L;
+        if (lp_after) Li.lines_stage = 1;
         int ni = std::min(step, n - i0);
         if (hio && g.level == 0) {
           // the input stage runs slice by slice as the slices land
@@ -794,6 +798,32 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
           return fail_cuda(err, "cascade launch");
         }
         i0 += ni;
+      }
+      for (int i0 = 0; lp_after && i0 < n; i0 += 65535) {
+        CascadeLaunch Li = L;
+        Li.lines_stage = 2;
+        const int ni = std::min(65535, n - i0);
+        Li.img0 = L.img0 + i0;
+        if (Li.src) Li.src = L.src + (size_t)i0 * L.src_stride;
+        if (Li.dst) Li.dst = L.dst + (size_t)i0 * L.dst_stride;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (timed && gi < a.max_groups) {
+          cudaEventCreate(&e0);
+          cudaEventCreate(&e1);
+          cudaEventRecord(e0, gs);
+        }
+        err = g.lines(Li, F, ni, gs);
+        if (e0) {
+          cudaEventRecord(e1, gs);
+          evs.push_back({gi, {e0, e1}});
+        }
+        if (err != cudaSuccess) {
+          for (auto& e : evs) {
+            cudaEventDestroy(e.second.first);
+            cudaEventDestroy(e.second.second);
+          }
+          return fail_cuda(err, "cascade launch");
+        }
       }
       if (hio && !g.out_runs.empty()) {
         // this group's channels are final for its images: copy them out
@@ -1678,7 +1708,7 @@ extern "C" int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int te
   const kym::Group& g = plan->p.groups[group];
   if (tensor_cores && g.tc_on && g.tcdft && kym::g_use_tcdft.load()) return 2;  // fold pass, GEMM kernel
   if (tensor_cores && g.tc_on && g.has_tc) return 1;
-  if (g.lines) return g.L.modulus ? 4 : 3;  // rows, columns, [rows + fold], low-pass
+  if (g.lines) return g.L.modulus ? 4 : 3;  // rows, columns, [rows + fold], low-pass (per sub-launch, or once after them)
   return 1;
 }
 
@@ -1699,9 +1729,14 @@ extern "C" int kym_s2d_group_launches(const kym_s2d_plan* plan, int group, int b
     const int step = (int)std::max(1.0, std::min(65535.0, 64.0 * 1024 * 1024 / slot_bytes));
     return (n + step - 1) / step;
   };
-  if (g.level == 0) return k * sub(batch);
+  // with several sub-launches, the low-pass kernel runs once after them
+  auto per = [&](int n) {
+    const int s = sub(n);
+    return s > 1 ? (k - 1) * s + (n + 65534) / 65535 : k * s;
+  };
+  if (g.level == 0) return per(batch);
   int tot = 0;
-  for (int c0 = 0; c0 < batch; c0 += chunk) tot += k * sub(std::min(chunk, batch - c0));
+  for (int c0 = 0; c0 < batch; c0 += chunk) tot += per(std::min(chunk, batch - c0));
   return tot;
 }
 

@@ -85,6 +85,7 @@ struct CascadeLaunch {
   long long ysave_stride;
   long long bsum_off;   // line-split modulus groups: folded low-pass blocks at dst + img * dst_stride + bsum_off
   unsigned char* opnd;  // DFT-GEMM form: per-path operand slots of the launch (image-major, then task)
+  int lines_stage;      // line-split groups: 0 every pass, 1 the line passes only, 2 the low-pass kernel only
 };
 
 }  // namespace kym
