@@ -48,13 +48,13 @@ int kym_set_specialized(int enable);
 int kym_set_tc_dft(int enable);
 
 /* Forwards after this call run the launch groups that do not depend on the
- * heaviest order-1 scale (the other order-1 scales and their order-2 groups)
- * on a low-priority side stream of the plan, forked from and joined back to
- * the caller's stream around every chunk, so that their blocks fill the SMs
- * the main chain leaves idle (enable=1, the default), or every group on the
- * caller's stream (enable=0).  Results are identical either way.  Timed
- * forwards and the DFT-GEMM form run on one stream.  Returns the previous
- * setting.  No counterpart in the reference. */
+ * heaviest order-1 scale (the other order-1 scales that have children, and
+ * their order-2 groups) on a side stream of the plan, forked from and joined
+ * back to the caller's stream around every chunk, so that their blocks fill
+ * the SMs the main chain leaves idle (enable=1, the default), or every group
+ * on the caller's stream (enable=0).  Results are identical either way.
+ * Timed forwards and the DFT-GEMM form run on one stream.  Returns the
+ * previous setting.  No counterpart in the reference. */
 int kym_set_side_lane(int enable);
 
 /* ------------------------------------------------------------------------
@@ -123,14 +123,19 @@ int kym_s2d_forward_tc(const kym_s2d_plan* plan, const float* x, float* out, int
  * cascade (host buffers page-locked; pageable ones give the same result
  * without the overlap).  lowpass_rows / lowpass_cols / status as in
  * kym_s2d_forward_tc select the tensor-core form; all three NULL the plain
- * form.  Ordered on `stream`: work enqueued there after this call sees
- * out_host complete.  No counterpart in the reference, whose frontend takes
- * tensors on the module's device (kymatio/scattering2d/frontend/
- * torch_frontend.py:72-111). */
+ * form.  The input copy starts once the work already on `stream` is done, or,
+ * when x_dev_free (a cudaEvent_t) is given, once that event has completed: a
+ * caller that rotates two staging buffers passes the event it recorded after
+ * the previous call on the same buffers (x_dev and out_dev), and the copy
+ * then overlaps the cascade of the call in between.  Ordered on `stream`: work enqueued there
+ * after this call sees out_host complete.  No counterpart in the reference,
+ * whose frontend takes tensors on the module's device (kymatio/scattering2d/
+ * frontend/torch_frontend.py:72-111). */
 int kym_s2d_forward_host(const kym_s2d_plan* plan, const float* x_host, float* out_host, int batch,
                          const float* const* filters, int n_filters, const float* const* lowpass_rows,
                          const float* const* lowpass_cols, int n_lowpass, unsigned* status, float* x_dev,
-                         float* out_dev, void* workspace, size_t workspace_bytes, int parts, void* stream);
+                         float* out_dev, void* workspace, size_t workspace_bytes, int parts, void* x_dev_free,
+                         void* stream);
 /* Tensor-core form of launch group `group` in kym_s2d_forward_tc: 0 none
  * (FP32 kernel), 1 the low-pass product on tcgen05, 2 the DFT-GEMM form. */
 int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group);

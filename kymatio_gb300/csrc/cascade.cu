@@ -253,8 +253,10 @@ struct DeviceState {
   float2* tw = nullptr;
   BwdTask* btasks = nullptr;
   GatherItem* gather = nullptr;
-  cudaStream_t copy_in = nullptr, copy_out = nullptr;  // host transfers of kym_s2d_forward_host
-  cudaStream_t side = nullptr;  // low-priority lane of the forward's independent group chains
+  // host transfers of kym_s2d_forward_host: input; output of the groups of
+  // each launch lane (a lane's copies wait only for its own groups)
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, copy_out_side = nullptr;
+  cudaStream_t side = nullptr;  // second lane of the forward's independent group chains
 };
 
 // Backward launch group: mirrors one forward group's geometry.
@@ -312,6 +314,7 @@ struct CascadePlan {
       cudaFree(kv.second.gather);
       if (kv.second.copy_in) cudaStreamDestroy(kv.second.copy_in);
       if (kv.second.copy_out) cudaStreamDestroy(kv.second.copy_out);
+      if (kv.second.copy_out_side) cudaStreamDestroy(kv.second.copy_out_side);
       if (kv.second.side) cudaStreamDestroy(kv.second.side);
     }
     if (have) cudaSetDevice(cur);
@@ -372,8 +375,11 @@ static int finalize_groups(CascadePlan* P) {
   };
   // launch lanes: an order-1 group and the order-2 groups reading its parent
   // spectra form a chain; the heaviest chain runs on the caller's stream,
-  // the others on a low-priority side stream, where their blocks fill the
-  // SMs the first chain leaves idle (its tails and narrow launches)
+  // the other chains with children on a side stream, where their blocks fill
+  // the SMs the first chain leaves idle (its tails and narrow launches).  The
+  // childless order-1 groups stay on the caller's stream, last: a short group
+  // ends the forward, so little output is left to copy after the cascade
+  // (kym_s2d_forward_host)
   {
     const int ng = (int)P->groups.size();
     std::vector<int> chain(ng, -1);
@@ -403,7 +409,7 @@ static int finalize_groups(CascadePlan* P) {
       if (P->groups[i].level == 1 && (heavy < 0 || weight[i] > weight[heavy])) heavy = i;
     for (int i = 0; i < ng; ++i) {
       Group& g = P->groups[i];
-      g.lane = (chain[i] >= 0 && chain[i] != heavy) ? 1 : 0;
+      g.lane = (chain[i] >= 0 && chain[i] != heavy && !(g.level == 1 && childless(g))) ? 1 : 0;
     }
     for (int i = 0; i < ng; ++i)
       if (P->groups[i].level == 2 && chain[i] < 0) {
@@ -422,7 +428,8 @@ static int finalize_groups(CascadePlan* P) {
 }
 
 // The side lane of the forward on the current device (created on first use,
-// lowest priority; the plan's device tables must exist already).
+// at the lowest priority, the default streams' own; the plan's device tables
+// must exist already).
 static int side_stream(CascadePlan* P, cudaStream_t* side) {
   int d = 0;
   cudaError_t e = cudaGetDevice(&d);
@@ -446,7 +453,7 @@ static int side_stream(CascadePlan* P, cudaStream_t* side) {
 
 // The two copy streams of kym_s2d_forward_host on the current device
 // (created on first use; the plan's device tables must exist already).
-static int host_copy_streams(CascadePlan* P, cudaStream_t* in, cudaStream_t* out) {
+static int host_copy_streams(CascadePlan* P, cudaStream_t* in, cudaStream_t* out, cudaStream_t* out_side) {
   int d = 0;
   cudaError_t e = cudaGetDevice(&d);
   if (e != cudaSuccess) return fail_cuda(e, "host forward");
@@ -461,8 +468,11 @@ static int host_copy_streams(CascadePlan* P, cudaStream_t* in, cudaStream_t* out
     return fail_cuda(e, "copy stream");
   if (!s.copy_out && (e = cudaStreamCreateWithFlags(&s.copy_out, cudaStreamNonBlocking)) != cudaSuccess)
     return fail_cuda(e, "copy stream");
+  if (!s.copy_out_side && (e = cudaStreamCreateWithFlags(&s.copy_out_side, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail_cuda(e, "copy stream");
   *in = s.copy_in;
   *out = s.copy_out;
+  *out_side = s.copy_out_side;
   return KYM_OK;
 }
 
@@ -609,8 +619,9 @@ struct RunArgs {
   // copied to out_host on copy_out once the group writing it has finished
   const float* x_host = nullptr;
   float* out_host = nullptr;
-  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, copy_out_side = nullptr;
   int parts = 1;
+  cudaEvent_t x_free = nullptr;  // non-null: the input copy waits for it instead of for `stream`
   // non-null: groups of lane 1 run here, forked from and joined back to the
   // caller's stream around every chunk
   cudaStream_t side = nullptr;
@@ -662,7 +673,7 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
   if (timed)
     for (int i = 0; i < a.max_groups; ++i) a.group_ms[i] = 0.f;
   // host transfers: input slices [part0[p], part0[p + 1]) copied on copy_in
-  const bool hio = a.x_host && a.out_host && a.copy_in && a.copy_out;
+  const bool hio = a.x_host && a.out_host && a.copy_in && a.copy_out && a.copy_out_side;
   EventPool pool;
   const int parts = hio ? std::max(1, std::min(a.parts, batch)) : 1;
   std::vector<int> part0(parts + 1);
@@ -670,12 +681,17 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
   std::vector<cudaEvent_t> in_ev(parts, nullptr);
   int waited = 0;  // input slices `stream` already waits for
   if (hio) {
-    // the copies start after the work already on `stream` (earlier users of
-    // the device input and the host output)
-    cudaEvent_t start;
-    if ((err = pool.make(&start)) != cudaSuccess || (err = cudaEventRecord(start, stream)) != cudaSuccess ||
-        (err = cudaStreamWaitEvent(a.copy_in, start, 0)) != cudaSuccess ||
-        (err = cudaStreamWaitEvent(a.copy_out, start, 0)) != cudaSuccess)
+    // the input copy overwrites the device input once its earlier users are
+    // done: the work already on `stream`, or the caller's event (a staging
+    // buffer the caller rotates, free while this stream still runs other
+    // work).  The output copies follow the groups, hence that work too.
+    cudaEvent_t start = a.x_free;
+    if (!start && ((err = pool.make(&start)) != cudaSuccess || (err = cudaEventRecord(start, stream)) != cudaSuccess))
+      return fail_cuda(err, "host forward");
+    // (the caller's event also orders `stream`, for the device output, in
+    // case the earlier call ran on another stream)
+    if ((err = cudaStreamWaitEvent(a.copy_in, start, 0)) != cudaSuccess ||
+        (a.x_free && (err = cudaStreamWaitEvent(stream, start, 0)) != cudaSuccess))
       return fail_cuda(err, "host forward");
     for (int p = 0; p < parts; ++p) {
       const size_t off = (size_t)part0[p] * x_stride;
@@ -828,16 +844,17 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
       if (hio && !g.out_runs.empty()) {
         // this group's channels are final for its images: copy them out
         const int a0 = g.level == 0 ? L.img0 : c0;
+        const cudaStream_t co = gs == stream ? a.copy_out : a.copy_out_side;
         cudaEvent_t done;
         if ((err = pool.make(&done)) != cudaSuccess || (err = cudaEventRecord(done, gs)) != cudaSuccess ||
-            (err = cudaStreamWaitEvent(a.copy_out, done, 0)) != cudaSuccess)
+            (err = cudaStreamWaitEvent(co, done, 0)) != cudaSuccess)
           return fail_cuda(err, "host forward");
         const size_t plane = (size_t)P->out_nr * P->out_nc;
         for (const auto& r : g.out_runs) {
           const size_t off = (size_t)a0 * out_stride + r.first * plane;
           err = cudaMemcpy2DAsync(a.out_host + off, out_stride * sizeof(float), out + off, out_stride * sizeof(float),
                                   (size_t)(r.second - r.first) * plane * sizeof(float), n, cudaMemcpyDeviceToHost,
-                                  a.copy_out);
+                                  co);
           if (err != cudaSuccess) return fail_cuda(err, "host output copy");
         }
       }
@@ -852,9 +869,11 @@ static int run_core(CascadePlan* P, const float* x, float* out, int batch, const
   }
   if (hio) {
     // `stream` orders after every copy: later work on it sees out_host complete
-    cudaEvent_t fin;
+    cudaEvent_t fin, fin_side;
     if ((err = wait_inputs(batch)) != cudaSuccess || (err = pool.make(&fin)) != cudaSuccess ||
-        (err = cudaEventRecord(fin, a.copy_out)) != cudaSuccess || (err = cudaStreamWaitEvent(stream, fin, 0)) != cudaSuccess)
+        (err = cudaEventRecord(fin, a.copy_out)) != cudaSuccess || (err = cudaStreamWaitEvent(stream, fin, 0)) != cudaSuccess ||
+        (err = pool.make(&fin_side)) != cudaSuccess || (err = cudaEventRecord(fin_side, a.copy_out_side)) != cudaSuccess ||
+        (err = cudaStreamWaitEvent(stream, fin_side, 0)) != cudaSuccess)
       return fail_cuda(err, "host forward");
   }
   if (timed) {
@@ -874,7 +893,7 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
                     int nfilters, void* workspace, size_t ws_bytes, cudaStream_t stream,
                     float* group_ms = nullptr, int max_groups = 0, const LowpassTable* lp = nullptr,
                     unsigned* status = nullptr, float2* ysave = nullptr, const float* x_host = nullptr,
-                    float* out_host = nullptr, int parts = 1) {
+                    float* out_host = nullptr, int parts = 1, cudaEvent_t x_free = nullptr) {
   if (!P || !x || !out || batch < 0) {
     set_error_message("forward", "null plan, input or output");
     return KYM_ERR_INVALID;
@@ -926,11 +945,12 @@ static int run_plan(CascadePlan* P, const float* x, float* out, int batch, const
       set_error_message("host forward", "null host input or output");
       return KYM_ERR_INVALID;
     }
-    rc = host_copy_streams(P, &a.copy_in, &a.copy_out);
+    rc = host_copy_streams(P, &a.copy_in, &a.copy_out, &a.copy_out_side);
     if (rc) return rc;
     a.x_host = x_host;
     a.out_host = out_host;
     a.parts = parts;
+    a.x_free = x_free;
   }
   return run_core(P, x, out, batch, F, a, stream);
 }
@@ -1666,7 +1686,7 @@ extern "C" int kym_s2d_forward_host(const kym_s2d_plan* plan, const float* x_hos
                                     const float* const* filters, int n_filters, const float* const* lowpass_rows,
                                     const float* const* lowpass_cols, int n_lowpass, unsigned* status, float* x_dev,
                                     float* out_dev, void* workspace, size_t workspace_bytes, int parts,
-                                    void* stream) {
+                                    void* x_dev_free, void* stream) {
   if (!plan || !x_host || !out_host || !x_dev || !out_dev || parts < 1) {
     kym::set_error_message("forward_host", "null plan, host or device buffer, or parts < 1");
     return KYM_ERR_INVALID;
@@ -1684,7 +1704,8 @@ extern "C" int kym_s2d_forward_host(const kym_s2d_plan* plan, const float* x_hos
   }
   return kym::run_plan(const_cast<CascadePlan*>(&plan->p), x_dev, out_dev, batch, filters, n_filters, workspace,
                        workspace_bytes, static_cast<cudaStream_t>(stream), nullptr, 0, tc ? &lp : nullptr,
-                       tc ? status : nullptr, nullptr, x_host, out_host, parts);
+                       tc ? status : nullptr, nullptr, x_host, out_host, parts,
+                       static_cast<cudaEvent_t>(x_dev_free));
 }
 
 extern "C" int kym_s2d_group_uses_tc(const kym_s2d_plan* plan, int group) {

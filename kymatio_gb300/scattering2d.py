@@ -216,7 +216,10 @@ class Scattering2D(nn.Module):
         overlap the cascade; page-locked inputs (``x.pin_memory()``) overlap
         best.  Tensor-core form when ``tensor_cores``.  With ``sync=False`` the
         call returns once the work is queued on the current stream:
-        synchronise before reading the result."""
+        synchronise before reading the result; calls queued back to back
+        alternate between two device staging buffers kept by the module (for
+        the last batch size), so a call's input copy overlaps the previous
+        call's cascade."""
         if not torch.is_tensor(x) or x.is_cuda or x.dtype != torch.float32 or not x.is_contiguous():
             raise TypeError('forward_host takes a contiguous float32 CPU tensor.')
         hw = (self._M_padded, self._N_padded) if self.pre_pad else self.shape
@@ -236,21 +239,34 @@ class Scattering2D(nn.Module):
         if B == 0:
             return out
         with torch.cuda.device(dev):
-            x_dev = torch.empty((B,) + hw, dtype=torch.float32, device=dev)
-            out_dev = torch.empty((B, self._channels) + self._out_hw, dtype=torch.float32, device=dev)
+            ring = self.__dict__.get('_host_ring')
+            if ring is None or ring['key'] != (B, dev):
+                # two staging slots: (device input, device output, event after the last call using them)
+                ring = self.__dict__['_host_ring'] = {
+                    'key': (B, dev), 'turn': 0,
+                    'slots': [[torch.empty((B,) + hw, dtype=torch.float32, device=dev),
+                               torch.empty((B, self._channels) + self._out_hw, dtype=torch.float32, device=dev),
+                               None] for _ in range(2)]}
+            slot = ring['slots'][ring['turn']]
+            ring['turn'] ^= 1
+            x_dev, out_dev, free = slot
             ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, B)
             ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
-            stream = torch.cuda.current_stream(dev).cuda_stream
+            cur = torch.cuda.current_stream(dev)
             lr = lc = status = None
             if self.tensor_cores:
                 lr, lc = self._lowpass_ptrs()
                 status = self._tc_status.data_ptr()
             _lib.check(lib.kym_s2d_forward_host(plan.h, xb.data_ptr(), out.data_ptr(), B, self._filter_ptrs(),
                                                 self._n_filters, lr, lc, self.J, status, x_dev.data_ptr(),
-                                                out_dev.data_ptr(), ws.data_ptr(), ws_bytes, int(parts), stream),
+                                                out_dev.data_ptr(), ws.data_ptr(), ws_bytes, int(parts),
+                                                free.cuda_event if free is not None else None, cur.cuda_stream),
                        'kym_s2d_forward_host')
+            if free is None:
+                free = slot[2] = torch.cuda.Event()
+            free.record(cur)
             if sync:
-                torch.cuda.current_stream(dev).synchronize()
+                cur.synchronize()
         return out
 
     def group_times(self, x, steps=3):

@@ -38,12 +38,14 @@ def test_matches_device_forward(dev, tc, parts, chunk):
 
 def test_headline_size_async_steps(dev):
     """256x256 J=3 (line-split input stage and order-1 group), several steps
-    queued without synchronising, each into its own output."""
+    queued without synchronising, each into its own output: the calls
+    alternate between the module's two staging buffers, each input copy
+    overlapping the previous call's cascade."""
     from kymatio_gb300 import Scattering2D
     S = Scattering2D(3, (256, 256)).to(dev)
     S.tensor_cores = True
     xs = [torch.from_numpy(np.random.default_rng(10 + i).random((3, 256, 256)).astype(np.float32)).pin_memory()
-          for i in range(3)]
+          for i in range(5)]
     outs = [S.forward_host(x, parts=2, sync=False) for x in xs]
     torch.cuda.synchronize()
     for x, o in zip(xs, outs):
