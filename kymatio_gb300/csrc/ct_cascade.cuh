@@ -84,7 +84,7 @@ __device__ __forceinline__ void ct_load(float2* A, const CascadeLaunch& L, const
     const float4* src4 = reinterpret_cast<const float4*>(L.src + (size_t)img * L.src_stride + t.src_off);
     const float2* psi2 = reinterpret_cast<const float2*>(F.f[t.psi]);
     const float sc = L.load_scale;
-    if constexpr (!ONED && C == 1 && MR % 2 == 0) {
+    if constexpr (!ONED && C == 1 && MR % 2 == 0 && (MR / 2 + 1) * (MC / 2) >= 2 * NT) {
       // The source is the spectrum of a real image, P x Q = KF MR x KF MC:
       // X[P - r][(Q - c) % Q] = conj X[r][c].  The aliases of row u' = MR - u
       // are the mirrors of row u's, (r, c) = (u + a MR, v + b MC), so one pass
@@ -92,6 +92,9 @@ __device__ __forceinline__ void ct_load(float2* A, const CascadeLaunch& L, const
       //   Y[u'][(MC - v) % MC] = sum conj X[r][c] psi[P - r][(Q - c) % Q]
       // (and column v + 1 -> MC - 1 - v): half the source loads per output.
       // Rows 0 and MR / 2 are their own mirrors and are folded directly.
+      // Taken where the half-size item set still gives every thread two
+      // items (68x68 and up at 512 threads); below that, fewer threads with
+      // longer load chains measured slower (20x20 and 40x40).
       constexpr int HC = MC / 2, NI = (MR / 2 + 1) * HC, P = KF * MR;
       const float* psi = F.f[t.psi];
 #pragma unroll 2
