@@ -73,69 +73,6 @@ __global__ void __launch_bounds__(NT, kLinesMinBlocks)
   const int img = blockIdx.z;
   const int r0 = blockIdx.x * RB;
   constexpr int NEL = RB * MC;
-  if constexpr (KF == 1 && RB == 16 && MR % 16 == 0 && MC % 2 == 0) {
-    // The source is the spectrum of a real image: X[MR - r][(MC - c) % MC] =
-    // conj X[r][c].  Block b takes the 8 rows d = 8b + 1 .. 8b + 8 (local
-    // 0..7) and their mirrors MR - d (local 8..15); the last block takes
-    // 7 rows, row 0 (local 7) and row MR / 2 (local 15), which are their own
-    // mirrors.  One load of X[d][c] gives both products:
-    //   Y[d][c] = X[d][c] psi[d][c],  Y[MR - d][(MC - c) % MC] = conj X[d][c] psi[MR - d][(MC - c) % MC]
-    constexpr int NB = MR / 16, HC = MC / 2;
-    const bool last = blockIdx.x == NB - 1;
-    const int nload = last ? 9 : 8;  // loaded local rows: 0..7 (and 15 in the last block)
-    auto grow = [&](int li) -> int {
-      const int b8 = 8 * (int)blockIdx.x + 1;
-      if (li < 8) return (last && li == 7) ? 0 : b8 + li;
-      if (last && li == 15) return MR / 2;
-      return MR - (b8 + li - 8);
-    };
-    const float4* src4 = reinterpret_cast<const float4*>(L.src + (size_t)img * L.src_stride + t.src_off);
-    const float* psi = F.f[t.psi];
-    const float2* psi2 = reinterpret_cast<const float2*>(psi);
-    const float sc = L.load_scale;
-    constexpr int PER = (9 * HC + NT - 1) / NT;
-    float4 sv[PER];
-    float2 fv[PER];
-    float gv0[PER], gv1[PER];
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      const int e = threadIdx.x + i * NT;
-      if (e < nload * HC) {
-        const int li = e / HC == 8 ? 15 : e / HC, v = 2 * (e % HC);
-        const int d = grow(li);
-        const size_t half = ((size_t)d * MC + v) >> 1;
-        sv[i] = __ldg(src4 + half);
-        fv[i] = __ldg(psi2 + half);
-        if (li < 8 && !(last && li == 7)) {
-          const float* prow = psi + (size_t)(MR - d) * MC;
-          gv0[i] = __ldg(prow + (MC - v) % MC);
-          gv1[i] = __ldg(prow + (MC - 1 - v));
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      const int e = threadIdx.x + i * NT;
-      if (e < nload * HC) {
-        const int li = e / HC == 8 ? 15 : e / HC, v = 2 * (e % HC);
-        const float4 x = sv[i];
-        A[li * LDR + v] = make_float2(x.x * fv[i].x * sc, x.y * fv[i].x * sc);
-        A[li * LDR + v + 1] = make_float2(x.z * fv[i].y * sc, x.w * fv[i].y * sc);
-        if (li < 8 && !(last && li == 7)) {
-          A[(li + 8) * LDR + (MC - v) % MC] = make_float2(x.x * gv0[i] * sc, -x.y * gv0[i] * sc);
-          A[(li + 8) * LDR + (MC - 1 - v)] = make_float2(x.z * gv1[i] * sc, -x.w * gv1[i] * sc);
-        }
-      }
-    }
-    __syncthreads();
-    ct::fft_lines<MC, RB, NT>(ct::RowLines<LDR, false>{A}, 0, L.prow.tw, L.modulus != 0);
-    float2* slot = L.dst + (size_t)img * L.dst_stride + t.dst_off;
-    for (int e = threadIdx.x; e < NEL; e += NT) {
-      const int li = e / MC, v = e % MC;
-      slot[(size_t)grow(li) * MC + v] = A[li * LDR + v];
-    }
-    return;
-  }
   if (KF == 0 || (KF < 0 && L.src_image)) {
     // reflect-padded image rows, every load of a thread in flight before the first store
     const float* x = L.x + (size_t)(L.img0 + img) * L.x_stride;
