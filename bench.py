@@ -761,16 +761,19 @@ def run_ours(args, world, rank, local):
     Mp = ((SIDE + 2 ** J) // 2 ** J + 1) * 2 ** J
     # algorithmic bytes of one launch: every source spectrum once per image (an
     # order-1 group reads the input spectrum, an order-2 group its ntasks / L
-    # parents), the output channels, the parent spectra an order-1 group
-    # writes, and the filters once per launch
+    # parents) -- the non-redundant half of it, rows 0 .. P/2, a real image's
+    # spectrum being Hermitian (the fold reads that much) --, the output
+    # channels, the parent spectra an order-1 group writes, and each distinct
+    # filter once per launch (L wavelets, one low-pass)
     if lvl == 0:
         bytes_launch = imgs_per_launch * (4 * SIDE * SIDE + 8 * rows * cols + 4 * side_out ** 2)
     else:
         src = fold * fold * rows * cols
+        src_half = (fold * rows // 2 + 1) * fold * cols
         n_src = 1 if lvl == 1 else max(1, ntasks // L)
         spill_w = ntasks * 8 * rows * cols if (lvl == 1 and not uses_tc and J > 1 and rows > (Mp >> (J - 1))) else 0
-        bytes_launch = imgs_per_launch * (n_src * 8 * src + ntasks * 4 * side_out ** 2 + spill_w) + \
-            ntasks * (4 * src + 4 * rows * cols)
+        bytes_launch = imgs_per_launch * (n_src * 8 * src_half + ntasks * 4 * side_out ** 2 + spill_w) + \
+            min(ntasks, L) * 4 * src + 4 * rows * cols
     dur_s = per_launch[dom] / 1e3
     hbm_peak = CTX['hbm_gbs']
     achieved = bytes_launch / dur_s / 1e9
