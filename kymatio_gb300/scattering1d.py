@@ -246,7 +246,11 @@ class Scattering1D(nn.Module):
             return self._scattering_unaveraged(x)
         batch_shape = x.shape[:-1]
         xb = x.reshape((-1, x.shape[-1]))
-        S = _autograd.CascadeFn.apply(xb, self)
+        # the autograd node only when a gradient can flow (it costs host time per call)
+        if torch.is_grad_enabled() and xb.requires_grad:
+            S = _autograd.CascadeFn.apply(xb, self)
+        else:
+            S = self._forward_raw(xb)
         S = S.reshape(tuple(batch_shape) + tuple(S.shape[-2:]))
         if self.out_type == 'array':
             return S

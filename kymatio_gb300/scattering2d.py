@@ -9,6 +9,8 @@ dicts with 'coef', 'j', 'n', 'theta') follow the reference.  The transform
 itself is one fused CUDA cascade (kym_s2d_forward) on the tensor's device
 and torch's current stream; CPU tensors are rejected, there is no fallback.
 """
+import contextlib
+
 import torch
 import torch.nn as nn
 
@@ -120,7 +122,24 @@ class Scattering2D(nn.Module):
                         meta.append({'j': (p1['j'], p2['j']), 'n': (n1, n2), 'theta': (p1['theta'], p2['theta'])})
         return meta
 
+    def __setattr__(self, name, value):
+        super().__setattr__(name, value)
+        if name.startswith('tensor') or name.startswith('lowpass_'):
+            self.__dict__['_buf_version'] = self.__dict__.get('_buf_version', 0) + 1
+
+    def _apply(self, fn, *args, **kwargs):
+        # .to() / .cuda() / .float() may move or replace the buffers
+        r = super()._apply(fn, *args, **kwargs)
+        self.__dict__['_buf_version'] = self.__dict__.get('_buf_version', 0) + 1
+        return r
+
     def _filter_ptrs(self):
+        # fast path: the buffers have not been moved or replaced since the
+        # table was built (in-place updates such as load_state_dict keep them)
+        ver = self.__dict__.get('_buf_version', 0)
+        fast = self.__dict__.get('_ptr_fast')
+        if fast is not None and fast[0] == ver and fast[1] == self.tensor0.data_ptr():
+            return fast[2]
         bufs = [getattr(self, 'tensor' + str(i)) for i in range(self._n_filters)]
         key = tuple(b.data_ptr() for b in bufs)
         if self._ptr_cache[0] != key:
@@ -129,6 +148,7 @@ class Scattering2D(nn.Module):
                     raise TypeError('The filters must be contiguous float32 CUDA tensors; call .cuda() on the '
                                     'module (the GB300 engine runs on CUDA only).')
             self._ptr_cache = (key, _lib.ptr_array(list(key)))
+        self.__dict__['_ptr_fast'] = (ver, key[0], self._ptr_cache[1])
         return self._ptr_cache[1]
 
     # -- forward ------------------------------------------------------------
@@ -158,7 +178,11 @@ class Scattering2D(nn.Module):
             raise TypeError('The input must be float32 (got %s).' % input.dtype)
         batch_shape = input.shape[:-2]
         x = input.reshape((-1,) + tuple(input.shape[-2:]))
-        S = _autograd.CascadeFn.apply(x, self)
+        # the autograd node only when a gradient can flow (it costs host time per call)
+        if torch.is_grad_enabled() and x.requires_grad:
+            S = _autograd.CascadeFn.apply(x, self)
+        else:
+            S = self._forward_raw(x)
         S = S.reshape(tuple(batch_shape) + tuple(S.shape[-3:]))
         if self.out_type == 'array':
             return S
@@ -191,7 +215,7 @@ class Scattering2D(nn.Module):
         out = torch.empty((B, self._channels) + self._out_hw, dtype=torch.float32, device=x.device)
         if B == 0:
             return out
-        with torch.cuda.device(x.device):
+        with _on_device(x.device):
             ptrs = self._filter_ptrs()
             ws_bytes = lib.kym_s2d_workspace_bytes(plan.h, B)
             ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=x.device)
@@ -343,6 +367,13 @@ class Scattering2D(nn.Module):
     def extra_repr(self):
         return 'J={}, shape={}, L={}, max_order={}, pre_pad={}, out_type={!r}'.format(
             self.J, self.shape, self.L, self.max_order, self.pre_pad, self.out_type)
+
+
+def _on_device(device):
+    """torch.cuda.device(device), skipped when it is already current."""
+    if device.index is None or device.index == torch.cuda.current_device():
+        return contextlib.nullcontext()
+    return torch.cuda.device(device)
 
 
 class _Plan:
