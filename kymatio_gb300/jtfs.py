@@ -358,8 +358,11 @@ class TimeFrequencyScattering(Scattering1D):
         return S
 
     # -- metadata -----------------------------------------------------------------------
-    def meta(self):
-        """kymatio/scattering1d/frontend/base_frontend.py:650-698."""
+    def _path_table(self):
+        """The output paths of the cascade, in output order, without data: the
+        generators run over a backend whose ops return None, and each path's
+        dict keeps its indices (n, n_fr, j, and the stacked n1 axis
+        n1_max / n1_stride in the 'joint' format)."""
         nd = _NoData()
 
         def blank(meta, n_levels):
@@ -374,37 +377,44 @@ class TimeFrequencyScattering(Scattering1D):
                                                filters_fr, self.log2_stride_fr, self.average_fr == 'local')
         S_gen = jtfs_average_and_format(U_gen, nd, filters[0], self.log2_stride, self.average, filters_fr[0],
                                         self.log2_stride_fr, self.average_fr, self.out_type, self.format)
-        paths = sorted(S_gen, key=lambda p: (len(p['n']), p['n']))
-        meta = {'key': [p['n'] for p in paths], 'n': [], 'n_fr': [], 'order': []}
-        for p in paths:
-            n = p['n']
-            if len(n) == 0:
-                if not (self.format == 'joint' and self.out_type == 'array'):
-                    meta['n'].append([np.nan, np.nan])
-                    meta['n_fr'].append(np.nan)
-                    meta['order'].append(0)
-                continue
-            if len(n) == 1:
-                meta['n'].append([range(0, p['n1_max'], p['n1_stride']), np.nan])
-            elif len(n) == 2 and self.format == 'joint':
-                meta['n'].append([range(0, p['n1_max'], p['n1_stride']), n[0]])
-            elif len(n) == 2:
-                meta['n'].append([n[0], np.nan])
-            else:
-                meta['n'].append(list(n[:2]))
-            meta['n_fr'].append(p['n_fr'][0])
-            meta['order'].append(len(n) - (self.format == 'time'))
-        meta['n'] = np.array(meta['n'], dtype=object)
-        meta['n_fr'] = np.array(meta['n_fr'])
-        meta['order'] = np.array(meta['order'])
-        for key in ['xi', 'sigma', 'j']:
-            meta[key] = np.zeros((meta['n_fr'].shape[0], 2)) * np.nan
-            for order, bank in enumerate(filters[1:]):
-                for k, psi in enumerate(bank):
-                    meta[key][meta['n'][:, order] == k, order] = psi[key]
-            meta[key + '_fr'] = meta['n_fr'] * np.nan
-            for n_fr, psi in enumerate(self.psis_fr_f):
-                meta[key + '_fr'][meta['n_fr'] == n_fr] = psi[key]
+        return sorted(S_gen, key=lambda p: (len(p['n']), p['n']))
+
+    def meta(self):
+        """Description of every output path, with the fields of kymatio's
+        TimeFrequencyScattering.meta (kymatio/scattering1d/frontend/
+        base_frontend.py:650-698): 'key' (every path's n), and per row
+        'n' = (n1, n2) -- the time-wavelet indices, n1 a range over the
+        stacked first-order axis in the 'joint' format, NaN where a path has
+        no such wavelet --, 'n_fr', 'order' (the number of time wavelets),
+        the time filters' 'xi' / 'sigma' / 'j' (two columns), the frequential
+        filter's 'xi_fr' / 'sigma_fr' / 'j_fr' and its 'spin'.  One row per
+        path of the path table, except the zeroth order in the 'joint'
+        format's array output, which holds no such row."""
+        paths = self._path_table()
+        rows = [p for p in paths if p['n'] or not (self.format == 'joint' and self.out_type == 'array')]
+        nan = np.nan
+
+        def indices(p):
+            # (n1, n2, n_fr) of a row; None where the path has no such filter
+            if not p['j']:
+                return None, None, None
+            n1 = range(0, p['n1_max'], p['n1_stride']) if 'n1_max' in p else p['n'][0]
+            n2 = p['n'][-2] if len(p['j']) == 2 else None
+            return n1, n2, p['n_fr'][0]
+
+        table = [indices(p) for p in rows]
+
+        def field(bank, i, name):
+            return bank[i][name] if isinstance(i, (int, np.integer)) else nan
+
+        meta = {'key': [p['n'] for p in paths],
+                'n': np.array([[nan if v is None else v for v in t[:2]] for t in table], dtype=object),
+                'n_fr': np.array([nan if t[2] is None else t[2] for t in table], dtype=float),
+                'order': np.array([len(p['j']) for p in rows])}
+        for name in ('xi', 'sigma', 'j'):
+            meta[name] = np.array([[field(self.psi1_f, t[0], name), field(self.psi2_f, t[1], name)]
+                                   for t in table], dtype=float).reshape(len(table), 2)
+            meta[name + '_fr'] = np.array([field(self.psis_fr_f, t[2], name) for t in table], dtype=float)
         meta['spin'] = np.sign(meta['xi_fr'])
         return meta
 

@@ -24,7 +24,8 @@ on current scipy) and writes:
 * ``ref_jtfs.npz`` -- seeded inputs and reference numpy FP64 outputs of joint
   time-frequency scattering (formats 'time' and 'joint', out_type array, list
   and dict, F local / zero / global, T global), with each configuration's
-  ``meta()`` (keys, order, n_fr, spin, frequential xi / sigma / j) and, for
+  ``meta()`` (keys, n, order, n_fr, spin, time and frequential xi / sigma /
+  j) and, for
   the array outputs, an upstream gradient and the reference torch frontend's
   float64 input gradient.
 
@@ -179,6 +180,17 @@ CASES_JTFS = [
 ]
 
 
+def meta_n_json(n):
+    """meta['n'] rows as JSON: a range as its list, NaN as null, an index as int."""
+    def one(v):
+        if isinstance(v, range):
+            return list(v)
+        if isinstance(v, float) and v != v:
+            return None
+        return int(v)
+    return [[one(v) for v in row] for row in n]
+
+
 def jtfs(ref_root):
     sys.path.insert(0, ref_root)
     from kymatio.scattering1d.frontend.numpy_frontend import TimeFrequencyScatteringNumPy
@@ -208,7 +220,8 @@ def jtfs(ref_root):
             out[name + '/g'], out[name + '/gx'] = g, xt.grad.numpy()
         m = S.meta()
         out[name + '/meta/key'] = np.array(json.dumps([list(map(int, k)) for k in m['key']]))
-        for field in ('order', 'n_fr', 'spin', 'xi_fr', 'sigma_fr', 'j_fr'):
+        out[name + '/meta/n'] = np.array(json.dumps(meta_n_json(m['n'])))
+        for field in ('order', 'n_fr', 'spin', 'xi_fr', 'sigma_fr', 'j_fr', 'xi', 'sigma', 'j'):
             out[name + '/meta/' + field] = np.asarray(m[field], dtype=np.float64)
         meta.append(dict(name=name, kwargs=kw))
     out['meta'] = np.array(json.dumps(meta))

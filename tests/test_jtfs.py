@@ -139,9 +139,17 @@ def test_jtfs_meta(case):
     m = S.meta()
     name = case['name']
     assert [list(k) for k in m['key']] == json.loads(str(_D[name + '/meta/key']))
-    for field in ('order', 'n_fr', 'spin', 'xi_fr', 'sigma_fr', 'j_fr'):
+    for field in ('order', 'n_fr', 'spin', 'xi_fr', 'sigma_fr', 'j_fr', 'xi', 'sigma', 'j'):
         np.testing.assert_allclose(np.asarray(m[field], dtype=np.float64), _D[name + '/meta/' + field],
                                    rtol=1e-12, atol=0, equal_nan=True, err_msg=field)
+
+    def n_json(v):  # a range as its list, NaN as null, an index as int
+        if isinstance(v, range):
+            return list(v)
+        if isinstance(v, float) and v != v:
+            return None
+        return int(v)
+    assert [[n_json(v) for v in row] for row in m['n']] == json.loads(str(_D[name + '/meta/n']))
     assert S.output_size() == len(m['key'])
 
 
