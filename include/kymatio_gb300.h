@@ -53,8 +53,12 @@ int kym_set_tc_dft(int enable);
  * back to the caller's stream around every chunk, so that their blocks fill
  * the SMs the main chain leaves idle (enable=1, the default), or every group
  * on the caller's stream (enable=0).  Results are identical either way.
- * Timed forwards and the DFT-GEMM form run on one stream.  Returns the
- * previous setting.  No counterpart in the reference. */
+ * Timed forwards and the DFT-GEMM form run on one stream.  The side stream
+ * (and the copy streams of kym_s2d_forward_host) belong to the plan and are
+ * shared by its callers: forwards of one plan from several host threads stay
+ * correct, but while one thread captures a CUDA graph from a plan, another
+ * must not run a forward of that plan.  Returns the previous setting.  No
+ * counterpart in the reference. */
 int kym_set_side_lane(int enable);
 
 /* ------------------------------------------------------------------------
