@@ -70,6 +70,45 @@ def test_plan_rejects_bad_geometry(lib):
     assert lib.kym_s2d_forward(None, None, None, 0, None, 0, None, 0, None) == _lib.KYM_ERR_INVALID
 
 
+def test_host_switches_and_argument_checks(lib):
+    """Host-side logic of the per-group tensor-core switch, the side-lane
+    switch, the launch counts and the host-buffer forward's argument checks
+    (no device work: every call here returns before touching CUDA)."""
+    from kymatio_gb300 import _lib
+    h = _lib._vp()
+    assert lib.kym_s2d_plan_create(256, 256, 3, 8, 2, 0, ctypes.byref(h)) == 0
+    ng = lib.kym_s2d_group_count(h)
+    assert ng == 7
+    assert lib.kym_s2d_set_group_tc(h, -1, 0) == -1 and lib.kym_s2d_set_group_tc(h, ng, 0) == -1
+    tc = [g for g in range(ng) if lib.kym_s2d_group_uses_tc(h, g) > 0]
+    assert tc, 'no tensor-core group at 256x256 J=3'
+    g = tc[0]
+    assert lib.kym_s2d_set_group_tc(h, g, 0) == 1
+    assert lib.kym_s2d_group_uses_tc(h, g) == 0 and lib.kym_s2d_group_kernels(h, g, 1) == 1
+    assert lib.kym_s2d_set_group_tc(h, g, 1) == 0 and lib.kym_s2d_group_uses_tc(h, g) > 0
+    prev = lib.kym_set_side_lane(0)
+    assert lib.kym_set_side_lane(prev) == 0
+    # the 272x272 line-split groups: the input stage in one sub-launch (3
+    # kernels); order 1 j1=0 in five sub-launches of 3 line passes, then one
+    # low-pass launch
+    assert lib.kym_s2d_group_launches(h, 0, 64, 1) == 3
+    assert lib.kym_s2d_group_launches(h, 1, 64, 1) == 3 * 5 + 1
+    buf = ctypes.create_string_buffer(64)
+    p = ctypes.cast(buf, _lib._vp)
+    ptrs = (_lib._vp * 1)(p)
+    args = dict(x_host=p, out_host=p, x_dev=p, out_dev=p)
+
+    def fwd(parts=1, lowpass=None, status=None, **kw):
+        a = dict(args, **kw)
+        return lib.kym_s2d_forward_host(h, a['x_host'], a['out_host'], 1, ptrs, 1, lowpass, lowpass, 1, status,
+                                        a['x_dev'], a['out_dev'], p, 64, parts, None, None)
+    for bad in ('x_host', 'out_host', 'x_dev', 'out_dev'):
+        assert fwd(**{bad: None}) == _lib.KYM_ERR_INVALID
+    assert fwd(parts=0) == _lib.KYM_ERR_INVALID
+    assert fwd(lowpass=ptrs) == _lib.KYM_ERR_INVALID  # tensor-core form without a status word
+    assert lib.kym_s2d_plan_destroy(h) == 0
+
+
 def test_product_bank_matches_reference():
     from kymatio_gb300.filter_bank import filter_bank_2d
     d = np.load(os.path.join(GOLDEN, 'ref_bank_2d.npz'))
