@@ -122,33 +122,23 @@ class Scattering2D(nn.Module):
                         meta.append({'j': (p1['j'], p2['j']), 'n': (n1, n2), 'theta': (p1['theta'], p2['theta'])})
         return meta
 
-    def __setattr__(self, name, value):
-        super().__setattr__(name, value)
-        if name.startswith('tensor') or name.startswith('lowpass_'):
-            self.__dict__['_buf_version'] = self.__dict__.get('_buf_version', 0) + 1
-
-    def _apply(self, fn, *args, **kwargs):
-        # .to() / .cuda() / .float() may move or replace the buffers
-        r = super()._apply(fn, *args, **kwargs)
-        self.__dict__['_buf_version'] = self.__dict__.get('_buf_version', 0) + 1
-        return r
-
     def _filter_ptrs(self):
-        # fast path: the buffers have not been moved or replaced since the
-        # table was built (in-place updates such as load_state_dict keep them)
-        ver = self.__dict__.get('_buf_version', 0)
-        fast = self.__dict__.get('_ptr_fast')
-        if fast is not None and fast[0] == ver and fast[1] == self.tensor0.data_ptr():
-            return fast[2]
-        bufs = [getattr(self, 'tensor' + str(i)) for i in range(self._n_filters)]
-        key = tuple(b.data_ptr() for b in bufs)
+        # the table is rebuilt whenever any buffer's address changed (.to(),
+        # reassignment, a swapped .data); the names are formatted once
+        names = self.__dict__.get('_filter_names')
+        if names is None or len(names) != self._n_filters:
+            names = self.__dict__['_filter_names'] = ['tensor' + str(i) for i in range(self._n_filters)]
+        bufs = self._buffers
+        key = tuple(bufs[n].data_ptr() for n in names)
+        if self._ptr_cache[0] == key:
+            return self._ptr_cache[1]
+        bufs = [getattr(self, n) for n in names]
         if self._ptr_cache[0] != key:
             for b in bufs:
                 if not b.is_cuda or b.dtype != torch.float32 or not b.is_contiguous():
                     raise TypeError('The filters must be contiguous float32 CUDA tensors; call .cuda() on the '
                                     'module (the GB300 engine runs on CUDA only).')
             self._ptr_cache = (key, _lib.ptr_array(list(key)))
-        self.__dict__['_ptr_fast'] = (ver, key[0], self._ptr_cache[1])
         return self._ptr_cache[1]
 
     # -- forward ------------------------------------------------------------
