@@ -160,6 +160,10 @@ int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores)
  * chunks and line-split sub-launches; tensor_cores as above).  No
  * counterpart in the reference (profiling). */
 int kym_s2d_group_launches(const kym_s2d_plan* plan, int group, int batch, int tensor_cores);
+/* Launch lane of group `group` in the forward (0: the caller's stream, 1: the
+ * plan's side stream, see kym_set_side_lane), or -1 for a bad group.  No
+ * counterpart in the reference (introspection). */
+int kym_s2d_group_lane(const kym_s2d_plan* plan, int group);
 
 /* Device build of the 2-D filter bank (replaces the host construction of
  * kymatio/scattering2d/filter_bank.py:5-175 called by ScatteringBase2D.

@@ -56,6 +56,7 @@ SIGNATURES = {
     'kym_s2d_group_uses_tc': (_c_int, [_vp, _c_int]),
     'kym_s2d_set_group_tc': (_c_int, [_vp, _c_int, _c_int]),
     'kym_set_side_lane': (_c_int, [_c_int]),
+    'kym_s2d_group_lane': (_c_int, [_vp, _c_int]),
     'kym_s2d_forward_host': (_c_int, [_vp, _vp, _vp, _c_int, ctypes.POINTER(_vp), _c_int, ctypes.POINTER(_vp),
                                       ctypes.POINTER(_vp), _c_int, _vp, _vp, _vp, _vp, _c_size, _c_int, _vp, _vp]),
     'kym_tc_selftest': (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _vp, _vp]),

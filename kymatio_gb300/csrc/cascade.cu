@@ -1724,6 +1724,11 @@ extern "C" int kym_s2d_set_group_tc(kym_s2d_plan* plan, int group, int enable) {
   return prev;
 }
 
+extern "C" int kym_s2d_group_lane(const kym_s2d_plan* plan, int group) {
+  if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
+  return plan->p.groups[group].lane;
+}
+
 extern "C" int kym_s2d_group_kernels(const kym_s2d_plan* plan, int group, int tensor_cores) {
   if (!plan || group < 0 || group >= (int)plan->p.groups.size()) return -1;
   const kym::Group& g = plan->p.groups[group];

@@ -109,6 +109,37 @@ def test_host_switches_and_argument_checks(lib):
     assert lib.kym_s2d_plan_destroy(h) == 0
 
 
+@pytest.mark.parametrize('side,J,lanes', [
+    # groups: input stage, order 1 by j1, then order 2 by (j1, j2)
+    (256, 3, [0, 0, 1, 0, 0, 0, 1]),
+    (128, 4, [0, 0, 1, 1, 0, 0, 0, 0, 1, 1, 1]),
+    (32, 2, [0, 0, 0, 0]),
+])
+def test_launch_lanes(lib, side, J, lanes):
+    """The heaviest order-1 scale and its order-2 groups stay on the caller's
+    stream; the other order-1 scales with children and their order-2 groups
+    go to the side lane; childless order-1 scales stay on the caller's stream.
+    Every order-2 group shares its parents' lane (they run in stream order)."""
+    from kymatio_gb300 import _lib
+    h = _lib._vp()
+    assert lib.kym_s2d_plan_create(side, side, J, 8, 2, 0, ctypes.byref(h)) == 0
+    ng = lib.kym_s2d_group_count(h)
+    got = [lib.kym_s2d_group_lane(h, g) for g in range(ng)]
+    assert got == lanes
+    assert lib.kym_s2d_group_lane(h, ng) == -1
+    info = []
+    for g in range(ng):
+        v = [ctypes.c_int() for _ in range(6)]
+        assert lib.kym_s2d_group_info(h, g, *[ctypes.byref(i) for i in v]) == 0
+        info.append((v[0].value, v[2].value, v[4].value))  # level, rows, fold
+    # an order-2 group of parent resolution rows * fold reads the order-1 group of that size
+    order1 = {rows: g for g, (lvl, rows, fold) in enumerate(info) if lvl == 1}
+    for g, (lvl, rows, fold) in enumerate(info):
+        if lvl == 2:
+            assert got[g] == got[order1[rows * fold]]
+    assert lib.kym_s2d_plan_destroy(h) == 0
+
+
 def test_product_bank_matches_reference():
     from kymatio_gb300.filter_bank import filter_bank_2d
     d = np.load(os.path.join(GOLDEN, 'ref_bank_2d.npz'))
